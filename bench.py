@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 strong-connectivity path.
+
+One step = one full SCC solve (trim -> first-pivot reach -> prefix-doubling
+multi-search -> partition -> finalise) of a seeded synthetic graph, the scope
+of the reference's `scc cost` (src/scc.cpp:62-66: graph load and transpose
+excluded).
+
+Default workload: directed 2-D kNN, 10^7 points uniform in the unit square
+(seed 2), k = 5 (m = 5e7), beta 1.5, tau 512, VGC on — the large-diameter
+plain-SCC configuration.  The graph (560 MB with its transpose) is larger than
+the 129 MB L2, so no flush is needed between steps.
+
+  value   edges/s with the graph resident in HBM (psc_scc_device), timed by
+          CUDA events on the library's stream around exactly K steps
+  e2e     edges/s through the C ABI with pinned host buffers: every step
+          uploads CSR + transpose (H2D), solves, and reads the labels (D2H)
+  roofline  the dominant kernel family of a profiled pass of the same
+          workload: algorithmic bytes / its event-timed duration vs the
+          measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (an OpenMP restatement of the reference's
+          SCC; the reference itself cannot be built) on the same graph
+
+`--impl reference` times that CPU implementation alone as the reference arm.
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU
+(replicas only: a solve does not shard); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "parallel-strong-connectivity_gb300"))
+
+WORKLOADS = {
+    "knn": dict(desc="directed 2-D kNN, 10^7 points in the unit square (seed 2), k=5",
+                make=lambda psc: psc.HostGraph.knn(10_000_000, 5, seed=2)),
+    "grid": dict(desc="directed 4096x4096 grid, fair-coin orientation, bidirectional p=0.3 (seed 2)",
+                 make=lambda psc: psc.HostGraph.grid(4096, 4096, 0.3, seed=2)),
+    "rmat16": dict(desc="directed R-MAT n=2^16, 2^20 draws (0.57,0.19,0.19,0.05), seed 1, dedup",
+                   make=lambda psc: psc.HostGraph.rmat(16, 1 << 20, seed=1)),
+    "rmat26": dict(desc="directed R-MAT n=2^26, 2^30 draws (0.57,0.19,0.19,0.05), seed 3, dedup",
+                   make=lambda psc: psc.HostGraph.rmat(26, 1 << 30, seed=3)),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"psc_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        try:
+            self.path.unlink()
+        except Exception:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+class Pinned:
+    """numpy views over page-locked host memory from the library."""
+
+    def __init__(self, lib):
+        self.lib = lib
+        self.ptrs = []
+
+    def empty(self, n, dtype):
+        dt = np.dtype(dtype)
+        p = C.c_void_p()
+        st = self.lib.psc_host_alloc(max(1, n * dt.itemsize), C.byref(p))
+        if st:
+            raise RuntimeError("pinned alloc failed")
+        self.ptrs.append(p.value)
+        buf = (C.c_byte * max(1, n * dt.itemsize)).from_address(p.value)
+        return np.frombuffer(buf, dtype=dt, count=n)
+
+    def copy(self, a):
+        out = self.empty(len(a), a.dtype)
+        out[:] = a
+        return out
+
+    def free(self):
+        for p in self.ptrs:
+            self.lib.psc_host_free(p)
+        self.ptrs = []
+
+
+def cpu_baseline(g, workload: str, budget_s: float = 15.0, max_runs: int = 20) -> dict:
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    runs, t_total = 0, 0.0
+    while runs < max_runs and (runs == 0 or t_total < budget_s):
+        t = time.perf_counter()
+        pyoracle.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=1, nthreads=threads)
+        t_total += time.perf_counter() - t
+        runs += 1
+    return {"value": g.m * runs / t_total, "unit": "edges/s", "cores": threads, "kind": "port",
+            "sample": f"{runs} full SCC solve(s) of the {workload} workload, "
+                      f"{t_total / runs * 1e3:.1f} ms each (OpenMP restatement of src/scc.hpp)"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_reference(args, world, rank, dist) -> None:
+    if rank != 0:
+        return
+    import psc
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    wl = WORKLOADS[args.workload]
+    g = wl["make"](psc)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        pyoracle.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=1, nthreads=threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        pyoracle.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=1, nthreads=threads)
+    dt = time.perf_counter() - t
+    value = g.m * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "SCC edges/s", "value": value, "unit": "edges/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"scc_{args.workload}", "graph": wl["desc"], "n": g.n, "m": g.m,
+                   "beta": 1.5, "tau": 512, "vgc": True},
+        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full SCC solves (OpenMP restatement of "
+                                   "src/scc.hpp; the reference needs the absent ParlayLib)"},
+        "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local, dist) -> None:
+    import psc
+    from psc import _lib
+
+    lib = psc.cuda()
+    if world > 1:
+        _lib.check(lib.psc_set_device(local), "psc_set_device")
+    if lib.psc_device_count() < 1:
+        raise SystemExit("no CUDA device")
+    wl = WORKLOADS[args.workload]
+    t = time.perf_counter()
+    g = wl["make"](psc)
+    log(f"[rank {rank}] generated {args.workload}: n={g.n} m={g.m} in {time.perf_counter() - t:.1f}s")
+    params = psc.default_params(seed=1)
+    n, m = g.n, g.m
+
+    pin = Pinned(lib)
+    h_off, h_E = pin.copy(g.off), pin.copy(g.E)
+    h_in_off, h_in_E = pin.copy(g.in_off), pin.copy(g.in_E)
+    h_labels = pin.empty(n, np.uint64)
+
+    dg = psc.DeviceGraph(g)
+    d_labels = C.c_void_p()
+    _lib.check(lib.psc_device_alloc(n * 8, C.byref(d_labels)), "psc_device_alloc")
+
+    # warm-up
+    for _ in range(args.warmup):
+        dg.scc_device(d_labels.value, params)
+    # correctness guard: device labels == host-call labels
+    ref_labels = dg.scc(params)
+    chk = pin.empty(n, np.uint64)
+    _lib.check(lib.psc_copy(chk.ctypes.data, d_labels.value, n * 8), "psc_copy")
+    if not np.array_equal(chk, ref_labels):
+        raise SystemExit("device and host SCC outputs disagree")
+
+    # timed region: exactly K steps, CUDA events on the library's stream
+    barrier(dist)
+    _lib.check(lib.psc_copy(None, None, 0), "sync")
+    launches = 0
+    with ClockSampler(local) as clk:
+        _lib.check(lib.psc_timer_start(dg.h), "psc_timer_start")
+        for _ in range(args.steps):
+            dg.scc_device(d_labels.value, params)
+            launches += dg.stats().kernel_launches
+        ms = C.c_double()
+        _lib.check(lib.psc_timer_stop(dg.h, C.byref(ms)), "psc_timer_stop")
+    barrier(dist)
+    total_ms = max_over_ranks(dist, ms.value)
+    clocks = clk.summary()
+    value = m * args.steps * world / (total_ms / 1e3)
+    last = dg.stats()
+
+    # profiled pass (same workload, after the timed region)
+    dg.set_profiling(True)
+    dg.profile_reset()
+    for _ in range(args.profile_steps):
+        dg.scc_device(d_labels.value, params)
+    prof = dg.profile()
+    dg.set_profiling(False)
+    fam, top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    peak, peak_kind = peaks()
+    achieved = (top["bytes"] / top["launches"]) / (top["ms"] / top["launches"] / 1e3) / 1e9 \
+        if top["launches"] and top["ms"] > 0 else 0.0
+    prof_total = sum(v["ms"] for v in prof.values())
+    roofline = {
+        "bound": "hbm", "kernel": fam, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+        "launches": top["launches"] // max(1, args.profile_steps),
+        "share": top["ms"] / prof_total if prof_total else None,
+        "bytes_per_launch": top["bytes"] / max(1, top["launches"]),
+    }
+
+    # end to end through the C ABI with pinned host buffers
+    h2d = h_off.nbytes + h_E.nbytes + h_in_off.nbytes + h_in_E.nbytes
+    d2h = n * 8
+    P = C.c_void_p
+
+    def e2e_step():
+        h = P()
+        _lib.check(lib.psc_graph_upload(h_off.ctypes.data, h_E.ctypes.data, h_in_off.ctypes.data,
+                                        h_in_E.ctypes.data, n, m, C.byref(h)), "psc_graph_upload")
+        try:
+            _lib.check(lib.psc_scc(h, C.byref(params), h_labels.ctypes.data), "psc_scc")
+        finally:
+            lib.psc_graph_free(h)
+
+    e2e_step()
+    if not np.array_equal(h_labels, ref_labels):
+        raise SystemExit("end-to-end SCC labels disagree")
+    barrier(dist)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t)
+    e2e_value = m * args.steps * world / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(g, args.workload)
+
+    lib.psc_device_free(d_labels.value)
+    dg.free()
+    pin.free()
+    if rank != 0:
+        return
+    line = {
+        "metric": "SCC edges/s", "value": value, "unit": "edges/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic",
+        "config": {"workload": f"scc_{args.workload}", "graph": wl["desc"], "n": n, "m": m,
+                   "beta": 1.5, "tau": 512, "vgc": True, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (no flush)" if (h2d > 129e6) else "L2-resident",
+                   "batches": last.batches, "subrounds": last.subrounds,
+                   "reach_rounds": last.reach_rounds},
+        "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / args.steps * 1e3},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["psc", "reference"], default="psc")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="knn")
+    ap.add_argument("--profile-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "psc":
+        log("note: fewer than 3 warm-up steps")
+    world, rank, local, dist = dist_setup()
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank, dist)
+        else:
+            run_gpu(args, world, rank, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

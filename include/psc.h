@@ -1,0 +1,139 @@
+/*
+ * psc.h — C ABI of the GB300 (sm_103a) strong-connectivity library
+ * (libpsc_cuda.so).  Plain pointers and sizes only; every call is
+ * host-synchronous and runs on the handle's own CUDA stream.  Distinct handles
+ * may be used from different threads at once; one handle is used by one
+ * thread at a time (the reference's SCC / REACH / LE_LIST objects are not
+ * thread-safe either, src/scc.hpp:38-115).
+ *
+ * Graph layout (struct Graph, src/graph.hpp:35-43): CSR offsets u64[n+1],
+ * targets u32[m], and the transpose in_off/in_E.  Vertex ids are u32.
+ *
+ * Return value: 0 (PSC_OK) or a PSC_ERR_* status; psc_strerror() names it.
+ * The reference returns no errors (I/O failures abort, a full label table is
+ * retried internally, src/scc.hpp:256-275); this library retries the same
+ * cases internally and reports only what it cannot recover from.
+ */
+#ifndef PSC_H
+#define PSC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PSC_OK = 0,
+  PSC_ERR_INVALID = 1,    /* bad argument */
+  PSC_ERR_OOM = 2,        /* device allocation failed */
+  PSC_ERR_CUDA = 3,       /* CUDA runtime error */
+  PSC_ERR_ITER_LIMIT = 4, /* a round loop exceeded its bound */
+  PSC_ERR_TABLE_FULL = 5, /* label table could not grow further */
+  PSC_ERR_NO_DEVICE = 6,  /* no usable CUDA device */
+  PSC_ERR_CAPACITY = 7    /* caller buffer too small (see the function) */
+};
+
+typedef struct psc_graph_s* psc_graph_t;
+
+/* Parameters of SCC (src/scc.cpp:40-55 flags and their defaults). */
+typedef struct {
+  double beta;         /* prefix-doubling growth, -beta (1.5) */
+  uint32_t tau;        /* VGC local-search budget, global `tau` (512) */
+  uint32_t lambda;     /* -lambda min bag size; device frontiers need no bag, accepted for parity */
+  int32_t local_reach; /* -local_reach: VGC in the first-pivot reach */
+  int32_t local_scc;   /* -local_scc: VGC in the multi-search */
+  uint64_t seed;       /* pivot permutation seed (stands in for parlay::random_shuffle) */
+  /* tuning knobs (0 = library default) */
+  uint32_t block;      /* threads per block of the expansion kernels */
+  uint32_t pull_div;   /* reach switches to pull when frontier edges > m / pull_div (20) */
+} psc_params_t;
+
+/* Fills the reference defaults: beta 1.5, tau 512, lambda 1024,
+ * local_reach = local_scc = 1 (the paper setting), seed 1. */
+void psc_params_default(psc_params_t* p);
+
+/* Uploads a CSR and its transpose (SCC's constructor, src/scc.hpp:81-92,
+ * holds the caller's Graph by reference; this copies it into HBM once).
+ * in_off/in_E may be NULL for a symmetric graph (transpose = itself). */
+int psc_graph_upload(const uint64_t* off, const uint32_t* E, const uint64_t* in_off,
+                     const uint32_t* in_E, uint64_t n, uint64_t m, psc_graph_t* out);
+/* Uploads a CSR and builds the transpose on the device
+ * (make_directed, src/graph.hpp:222-245). */
+int psc_graph_upload_directed(const uint64_t* off, const uint32_t* E, uint64_t n, uint64_t m,
+                              psc_graph_t* out);
+/* Same graph as psc_graph_upload, but the arrays are already in device memory
+ * of the current device; they are copied (device to device). */
+int psc_graph_upload_device(const uint64_t* d_off, const uint32_t* d_E, const uint64_t* d_in_off,
+                            const uint32_t* d_in_E, uint64_t n, uint64_t m, psc_graph_t* out);
+int psc_graph_free(psc_graph_t g);
+uint64_t psc_graph_num_vertices(psc_graph_t g);
+uint64_t psc_graph_num_edges(psc_graph_t g);
+/* Copies the device transpose back (in_off u64[n+1], in_E u32[m]). */
+int psc_graph_download_transpose(psc_graph_t g, uint64_t* in_off, uint32_t* in_E);
+
+/* SCC::scc (src/scc.hpp:277-476).  labels_out: host u64[n], the reference's
+ * sequence<size_t> (final value = (label & 0xFFFFFFFF) - 1). */
+int psc_scc(psc_graph_t g, const psc_params_t* p, uint64_t* labels_out);
+/* Same, labels left in device memory d_labels (u64[n]) of the handle's device. */
+int psc_scc_device(psc_graph_t g, const psc_params_t* p, uint64_t* d_labels);
+
+/* REACH::reach (src/reach.hpp:208-243): dst_out host u8[n], 1 = reachable
+ * from src.  dir 0 = forward (out-edges), 1 = backward (in-edges, as after
+ * REACH::swap_graph).  Returns rounds via *rounds if non-NULL. */
+int psc_reach(psc_graph_t g, uint32_t src, int dir, int local, uint32_t tau, uint8_t* dst_out,
+              uint32_t* rounds);
+
+/* Per-call statistics of the last psc_scc / psc_reach / psc_cc / psc_lelist
+ * on this handle. */
+typedef struct {
+  double total_ms;          /* device time of the call (CUDA events) */
+  uint64_t reach_rounds;    /* first-pivot forward + backward rounds */
+  uint64_t batches;         /* prefix-doubling batches run */
+  uint64_t subrounds;       /* multi-search sub-rounds, both directions */
+  uint64_t table_grows;     /* label-table rehashes */
+  uint64_t kernel_launches; /* kernels launched by the call */
+} psc_stats_t;
+int psc_last_stats(psc_graph_t g, psc_stats_t* out);
+
+/* Profiling of kernel families (off by default).  When on, every launch of
+ * family k is bracketed by CUDA events on the handle's stream and its
+ * algorithmic byte count is accumulated.  psc_profile_get returns, for family
+ * index k < psc_profile_count(), its name, launches, total ms and bytes. */
+int psc_set_profiling(psc_graph_t g, int on);
+int psc_profile_count(void);
+int psc_profile_get(psc_graph_t g, int k, const char** name, uint64_t* launches, double* ms,
+                    double* bytes);
+int psc_profile_reset(psc_graph_t g);
+
+/* Memory and timing plumbing for callers without a CUDA runtime of their own
+ * (ctypes, FFI).  No reference counterpart.
+ *   psc_host_alloc / psc_host_free     page-locked host memory (fast H2D/D2H)
+ *   psc_device_alloc / psc_device_free device memory on the current device
+ *   psc_copy(dst, src, bytes)          cudaMemcpy with the direction inferred
+ *   psc_timer_start / psc_timer_stop   CUDA events on the handle's stream;
+ *                                      stop waits and returns elapsed ms */
+int psc_host_alloc(size_t bytes, void** ptr);
+int psc_host_free(void* ptr);
+int psc_device_alloc(size_t bytes, void** ptr);
+int psc_device_free(void* ptr);
+int psc_copy(void* dst, const void* src, size_t bytes);
+int psc_timer_start(psc_graph_t g);
+int psc_timer_stop(psc_graph_t g, double* ms);
+
+/* Selects the CUDA device that later psc_graph_upload* calls on this thread
+ * bind to (cudaSetDevice of the library's runtime). */
+int psc_set_device(int device);
+
+/* Number of visible CUDA devices (0 when there is none or the driver is
+ * unusable).  No reference counterpart; lets callers probe before uploading. */
+int psc_device_count(void);
+
+const char* psc_strerror(int status);
+const char* psc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,324 @@
+// Device-side building blocks shared by every kernel of libpsc_cuda.so:
+// the graph handle, status codes, the workspace arena, warp-aggregated
+// frontier appends, the balanced warp edge expansion and the 64-bit
+// open-addressing (vertex, pivot) table.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/psc.h"
+#include "psc_hash.h"
+
+namespace psc {
+
+constexpr uint64_t kTopBit = 1ull << 32;       // src/scc.hpp:22
+constexpr uint64_t kValMask = 0xFFFFFFFFull;   // src/scc.hpp:23
+constexpr uint32_t kNone = 0xFFFFFFFFu;        // UINT_N_MAX
+constexpr uint64_t kEmpty = ~0ull;             // empty (vertex, pivot) slot
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kWarp = 32;
+// Frontier vertices with more out-edges than this are expanded by the whole
+// grid instead of by one warp.
+constexpr uint32_t kHeavyDeg = 8192;
+
+// ---------------------------------------------------------------------------
+// Kernel families for profiling (launch counts, event time, algorithmic bytes)
+// ---------------------------------------------------------------------------
+enum Family : int {
+  F_TRIM = 0,
+  F_REACH_PUSH,
+  F_REACH_PULL,
+  F_REACH_VGC,
+  F_HEAVY,
+  F_LABEL_FIRST,
+  F_COMPACT,
+  F_MS_SEED,
+  F_MS_EXPAND,
+  F_MS_VGC,
+  F_TABLE,
+  F_PARTITION,
+  F_FINALISE,
+  F_CC,
+  F_LE,
+  F_TRANSPOSE,
+  F_COUNT
+};
+extern const char* const kFamilyName[F_COUNT];
+
+// Device counters written by the round kernels and read back between rounds.
+struct Counters {
+  unsigned long long next;       // items appended to the next frontier
+  unsigned long long next_edges; // out-edges of the appended items (direction heuristic)
+  unsigned long long heavy;      // items sent to the heavy list
+  unsigned long long fail;       // failed table inserts (table needs to grow)
+  unsigned long long edges;      // edges scanned (algorithmic bytes)
+  unsigned long long probes;     // table slots probed (algorithmic bytes)
+  unsigned long long aux0;       // kernel-specific
+  unsigned long long aux1;
+};
+
+// ---------------------------------------------------------------------------
+// Host-side helpers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct ProfEntry {
+  uint64_t launches = 0;
+  double ms = 0;
+  double bytes = 0;
+};
+
+struct PendingEvent {
+  int fam;
+  cudaEvent_t a, b;
+  double bytes;
+};
+
+}  // namespace psc
+
+struct psc_graph_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t n = 0, m = 0;
+  bool symmetric = false;
+  uint64_t* off = nullptr;
+  uint32_t* E = nullptr;
+  uint64_t* in_off = nullptr;  // aliases off for symmetric graphs
+  uint32_t* in_E = nullptr;
+  int num_sms = 0;
+  // named scratch buffers, grown on demand (stream-ordered allocator)
+  std::vector<psc::DevBuf> bufs;
+  psc::Counters* ctr = nullptr;   // device
+  psc::Counters* hctr = nullptr;  // pinned host mirror
+  // statistics / profiling
+  psc_stats_t stats{};
+  bool profiling = false;
+  psc::ProfEntry prof[psc::F_COUNT];
+  std::vector<psc::PendingEvent> pending;
+  std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  cudaEvent_t u0 = nullptr, u1 = nullptr;  // caller timer (psc_timer_*)
+};
+
+namespace psc {
+
+// Scratch buffer slots (indices into psc_graph_s::bufs).
+enum Buf : int {
+  B_LABELS = 0,   // u64[n] labels when the caller passes host memory
+  B_P,            // u32[n] pivot order
+  B_CENTERS,      // u32[n]
+  B_FRONT,        // u32[n] batch pivots
+  B_VIS_F,        // u32[n/32] visited bitmap (forward)
+  B_VIS_B,        // u32[n/32] visited bitmap (backward)
+  B_QA,           // u32[n] vertex frontier A
+  B_QB,           // u32[n] vertex frontier B
+  B_FB_A,         // u32[n/32] frontier bitmap A
+  B_FB_B,         // u32[n/32] frontier bitmap B
+  B_HEAVY,        // heavy list
+  B_SCAN,         // scan scratch
+  B_TMP32,        // u32[n] misc
+  B_TF,           // forward label table
+  B_TB,           // backward label table
+  B_TS,           // spare table for rehash
+  B_PA,           // u64 pair frontier A
+  B_PB,           // u64 pair frontier B
+  B_PH,           // u64 pair heavy list
+  B_AUX0,
+  B_AUX1,
+  B_AUX2,
+  B_AUX3,
+  B_COUNT
+};
+
+// Status plumbing: PSC_TRY returns the status of a failing expression.
+#define PSC_TRY(expr)                 \
+  do {                                \
+    int _s = (expr);                  \
+    if (_s != PSC_OK) return _s;      \
+  } while (0)
+
+#define PSC_CUDA(expr)                                         \
+  do {                                                         \
+    cudaError_t _e = (expr);                                   \
+    if (_e != cudaSuccess) return ::psc::cuda_status(_e);      \
+  } while (0)
+
+int cuda_status(cudaError_t e);
+void set_last_cuda_error(cudaError_t e);
+
+// Returns a device pointer of at least `bytes` for slot `b` (contents of a
+// regrown buffer are not preserved).
+int ensure(psc_graph_s* g, int b, size_t bytes, void** out);
+template <class T>
+inline int ensure_t(psc_graph_s* g, int b, size_t count, T** out) {
+  void* p = nullptr;
+  int s = ensure(g, b, count * sizeof(T) + 16, &p);
+  *out = (T*)p;
+  return s;
+}
+// Swap two slots (ping-pong buffers).
+void swap_bufs(psc_graph_s* g, int a, int b);
+
+// Reads the device counters to the host mirror and waits for the stream.
+int read_counters(psc_graph_s* g);
+int zero_counters(psc_graph_s* g);
+
+// Profiling brackets (no-ops unless profiling is on).
+void prof_begin(psc_graph_s* g, int fam, cudaEvent_t* a);
+void prof_end(psc_graph_s* g, int fam, cudaEvent_t a, double bytes);
+int prof_flush(psc_graph_s* g);
+
+struct ProfScope {
+  psc_graph_s* g;
+  int fam;
+  cudaEvent_t a = nullptr;
+  double bytes = 0;
+  ProfScope(psc_graph_s* g_, int f) : g(g_), fam(f) {
+    g->stats.kernel_launches++;
+    prof_begin(g, fam, &a);
+  }
+  ~ProfScope() { prof_end(g, fam, a, bytes); }
+};
+
+inline unsigned grid_for(psc_graph_s* g, uint64_t items, unsigned block, unsigned per_thread = 1) {
+  uint64_t want = (items + (uint64_t)block * per_thread - 1) / ((uint64_t)block * per_thread);
+  uint64_t cap = (uint64_t)g->num_sms * 16;
+  if (want < 1) want = 1;
+  if (want > cap) want = cap;
+  return (unsigned)want;
+}
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ uint64_t ld_cg(const uint64_t* p) { return __ldcg((const unsigned long long*)p); }
+__device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) { return __ldcg(p); }
+
+// Warp-aggregated append: every lane of the (converged) warp calls it; lanes
+// with take == true receive consecutive slots of *counter.
+__device__ __forceinline__ unsigned long long warp_append(unsigned long long* counter, bool take) {
+  unsigned mask = __ballot_sync(kFull, take);
+  if (mask == 0) return 0;
+  unsigned lane = lane_id();
+  int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+  base = __shfl_sync(kFull, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// Warp sum of a u64 value.
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// Per-warp shared state of the balanced expansion.
+struct WarpExpandSmem {
+  uint32_t excl[32];
+  uint64_t beg[32];
+};
+
+// Balanced edge expansion over the 32 lanes' adjacency ranges [beg, beg+deg):
+// the warp walks the concatenation of the ranges 32 edges at a time, every
+// lane owning one edge per step (coalesced reads of E).  visit(src_lane, e)
+// returns nothing; all lanes call it with active == false past the end so
+// warp collectives inside visit stay converged.
+template <class Visit>
+__device__ __forceinline__ void warp_expand(WarpExpandSmem& sm, uint64_t beg, uint32_t deg,
+                                            Visit&& visit) {
+  const unsigned lane = lane_id();
+  uint32_t incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(kFull, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  sm.excl[lane] = incl - deg;
+  sm.beg[lane] = beg;
+  __syncwarp();
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t gi = base + lane;
+    const bool active = gi < total;
+    int src = 0;
+    uint64_t e = 0;
+    if (active) {
+      // largest lane s with excl[s] <= gi
+      int lo = 0, hi = 31;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (sm.excl[mid] <= gi)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      src = lo;
+      e = sm.beg[src] + (gi - sm.excl[src]);
+    }
+    visit(active, src, e);
+  }
+  __syncwarp();
+}
+
+// Insert key into a linear-probing table of 2^k slots.
+// Returns 1 if inserted, 0 if already present, -1 after `limit` probes.
+__device__ __forceinline__ int table_insert(unsigned long long* T, uint64_t mask, uint64_t key,
+                                            uint32_t limit, uint32_t* probes) {
+  uint64_t h = hash64(key) & mask;
+  for (uint32_t i = 0; i < limit; i++) {
+    uint64_t cur = __ldcg(&T[h]);
+    if (cur == key) {
+      *probes += i + 1;
+      return 0;
+    }
+    if (cur == kEmpty) {
+      uint64_t old = atomicCAS(&T[h], (unsigned long long)kEmpty, (unsigned long long)key);
+      if (old == kEmpty) {
+        *probes += i + 1;
+        return 1;
+      }
+      if (old == key) {
+        *probes += i + 1;
+        return 0;
+      }
+    }
+    h = (h + 1) & mask;
+  }
+  *probes += limit;
+  return -1;
+}
+
+__device__ __forceinline__ bool table_contains(const unsigned long long* T, uint64_t mask,
+                                               uint64_t key) {
+  uint64_t h = hash64(key) & mask;
+  for (uint64_t i = 0; i <= mask; i++) {
+    uint64_t cur = T[h];
+    if (cur == key) return true;
+    if (cur == kEmpty) return false;
+    h = (h + 1) & mask;
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool bit_test(const uint32_t* bm, uint32_t v) {
+  return (__ldcg(&bm[v >> 5]) >> (v & 31)) & 1u;
+}
+
+// Sets bit v; returns true if this call flipped it from 0 to 1.
+__device__ __forceinline__ bool bit_set(uint32_t* bm, uint32_t v) {
+  uint32_t b = 1u << (v & 31);
+  if (__ldcg(&bm[v >> 5]) & b) return false;
+  return !(atomicOr(&bm[v >> 5], b) & b);
+}
+
+}  // namespace psc

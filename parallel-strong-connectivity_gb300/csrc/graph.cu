@@ -1,0 +1,432 @@
+// Handle lifecycle, scratch buffers, counters, profiling and graph upload
+// for libpsc_cuda.so.  Declared in include/psc.h.
+#include <cstdio>
+#include <cstring>
+
+#include "common.cuh"
+#include "engines.cuh"
+#include "scan.cuh"
+
+namespace psc {
+
+const char* const kFamilyName[F_COUNT] = {
+    "trim",        "reach_push", "reach_pull", "reach_vgc", "heavy",     "label_first",
+    "compact",     "ms_seed",    "ms_expand",  "ms_vgc",    "table",     "partition",
+    "finalise",    "cc",         "lelist",     "transpose"};
+
+static thread_local cudaError_t g_last_cuda = cudaSuccess;
+
+void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+
+int cuda_status(cudaError_t e) {
+  g_last_cuda = e;
+  if (e == cudaErrorMemoryAllocation) return PSC_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return PSC_ERR_NO_DEVICE;
+  return PSC_ERR_CUDA;
+}
+
+int ensure(psc_graph_s* g, int b, size_t bytes, void** out) {
+  DevBuf& d = g->bufs[b];
+  if (d.bytes < bytes) {
+    if (d.p) PSC_CUDA(cudaFreeAsync(d.p, g->stream));
+    d.p = nullptr;
+    d.bytes = 0;
+    cudaError_t e = cudaMallocAsync(&d.p, bytes, g->stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      d.p = nullptr;
+      return cuda_status(e);
+    }
+    d.bytes = bytes;
+  }
+  *out = d.p;
+  return PSC_OK;
+}
+
+int ensure_keep(psc_graph_s* g, int b, size_t bytes, size_t keep, void** out) {
+  DevBuf& d = g->bufs[b];
+  if (d.bytes >= bytes) {
+    *out = d.p;
+    return PSC_OK;
+  }
+  void* np = nullptr;
+  cudaError_t e = cudaMallocAsync(&np, bytes, g->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_status(e);
+  }
+  if (d.p && keep) PSC_CUDA(cudaMemcpyAsync(np, d.p, keep, cudaMemcpyDeviceToDevice, g->stream));
+  if (d.p) PSC_CUDA(cudaFreeAsync(d.p, g->stream));
+  d.p = np;
+  d.bytes = bytes;
+  *out = np;
+  return PSC_OK;
+}
+
+void swap_bufs(psc_graph_s* g, int a, int b) { std::swap(g->bufs[a], g->bufs[b]); }
+
+int zero_counters(psc_graph_s* g) {
+  PSC_CUDA(cudaMemsetAsync(g->ctr, 0, sizeof(Counters), g->stream));
+  return PSC_OK;
+}
+
+int read_counters(psc_graph_s* g) {
+  PSC_CUDA(cudaMemcpyAsync(g->hctr, g->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, g->stream));
+  PSC_CUDA(cudaStreamSynchronize(g->stream));
+  return PSC_OK;
+}
+
+static cudaEvent_t pool_event(psc_graph_s* g) {
+  if (!g->event_pool.empty()) {
+    cudaEvent_t e = g->event_pool.back();
+    g->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void prof_begin(psc_graph_s* g, int, cudaEvent_t* a) {
+  if (!g->profiling) return;
+  *a = pool_event(g);
+  cudaEventRecord(*a, g->stream);
+}
+
+void prof_end(psc_graph_s* g, int fam, cudaEvent_t a, double bytes) {
+  if (!g->profiling || !a) return;
+  cudaEvent_t b = pool_event(g);
+  cudaEventRecord(b, g->stream);
+  g->pending.push_back(PendingEvent{fam, a, b, bytes});
+  if (g->pending.size() > 4096) prof_flush(g);
+}
+
+int prof_flush(psc_graph_s* g) {
+  if (g->pending.empty()) return PSC_OK;
+  PSC_CUDA(cudaStreamSynchronize(g->stream));
+  for (auto& p : g->pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    g->prof[p.fam].launches++;
+    g->prof[p.fam].ms += ms;
+    g->prof[p.fam].bytes += p.bytes;
+    g->event_pool.push_back(p.a);
+    g->event_pool.push_back(p.b);
+  }
+  g->pending.clear();
+  return PSC_OK;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tile_sums(uint64_t* a, uint64_t nt) {
+  __shared__ uint64_t sm[33];
+  uint64_t carry = 0;
+  for (uint64_t base = 0; base < nt; base += 1024) {
+    uint64_t i = base + threadIdx.x;
+    uint64_t v = i < nt ? a[i] : 0;
+    uint64_t tot;
+    uint64_t ex = block_excl_scan<1024>(v, sm, &tot);
+    if (i < nt) a[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) a[nt] = carry;
+}
+
+int call_begin(psc_graph_s* g) {
+  PSC_CUDA(cudaSetDevice(g->device));
+  std::memset(&g->stats, 0, sizeof(g->stats));
+  PSC_CUDA(cudaEventRecord(g->t0, g->stream));
+  return PSC_OK;
+}
+
+int call_end(psc_graph_s* g) {
+  PSC_CUDA(cudaEventRecord(g->t1, g->stream));
+  PSC_CUDA(cudaEventSynchronize(g->t1));
+  float ms = 0;
+  PSC_CUDA(cudaEventElapsedTime(&ms, g->t0, g->t1));
+  g->stats.total_ms = ms;
+  PSC_TRY(prof_flush(g));
+  PSC_CUDA(cudaGetLastError());
+  return PSC_OK;
+}
+
+static int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
+  int dev = 0;
+  PSC_CUDA(cudaGetDevice(&dev));
+  auto* g = new psc_graph_s();
+  g->device = dev;
+  g->n = n;
+  g->m = m;
+  g->bufs.resize(B_COUNT);
+  cudaError_t e;
+  if ((e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc(&g->ctr, sizeof(Counters))) != cudaSuccess ||
+      (e = cudaMallocHost(&g->hctr, sizeof(Counters))) != cudaSuccess ||
+      (e = cudaEventCreate(&g->t0)) != cudaSuccess || (e = cudaEventCreate(&g->t1)) != cudaSuccess ||
+      (e = cudaEventCreate(&g->u0)) != cudaSuccess || (e = cudaEventCreate(&g->u1)) != cudaSuccess) {
+    psc_graph_free(g);
+    return cuda_status(e);
+  }
+  // keep freed scratch in the pool between calls
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  *out = g;
+  return PSC_OK;
+}
+
+static int alloc_graph_arrays(psc_graph_s* g, bool symmetric) {
+  const uint64_t n = g->n, m = g->m;
+  g->symmetric = symmetric;
+  PSC_CUDA(cudaMalloc(&g->off, (n + 1) * sizeof(uint64_t)));
+  PSC_CUDA(cudaMalloc(&g->E, (m ? m : 1) * sizeof(uint32_t)));
+  if (symmetric) {
+    g->in_off = g->off;
+    g->in_E = g->E;
+  } else {
+    PSC_CUDA(cudaMalloc(&g->in_off, (n + 1) * sizeof(uint64_t)));
+    PSC_CUDA(cudaMalloc(&g->in_E, (m ? m : 1) * sizeof(uint32_t)));
+  }
+  return PSC_OK;
+}
+
+}  // namespace psc
+
+using namespace psc;
+
+extern "C" {
+
+void psc_params_default(psc_params_t* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->beta = 1.5;
+  p->tau = 512;
+  p->lambda = 1024;
+  p->local_reach = 1;
+  p->local_scc = 1;
+  p->seed = 1;
+}
+
+int psc_graph_upload(const uint64_t* off, const uint32_t* E, const uint64_t* in_off,
+                     const uint32_t* in_E, uint64_t n, uint64_t m, psc_graph_t* out) {
+  if (!out || !off || (m && !E) || n == 0 || n >= 0xFFFFFFFFull) return PSC_ERR_INVALID;
+  if ((in_off == nullptr) != (in_E == nullptr)) return PSC_ERR_INVALID;
+  if (off[0] != 0 || off[n] != m) return PSC_ERR_INVALID;
+  if (in_off && (in_off[0] != 0 || in_off[n] != m)) return PSC_ERR_INVALID;
+  psc_graph_s* g = nullptr;
+  PSC_TRY(make_handle(n, m, &g));
+  bool sym = in_off == nullptr;
+  int s = alloc_graph_arrays(g, sym);
+  if (s == PSC_OK) {
+    cudaError_t e = cudaMemcpy(g->off, off, (n + 1) * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && m) e = cudaMemcpy(g->E, E, m * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !sym) e = cudaMemcpy(g->in_off, in_off, (n + 1) * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !sym && m) e = cudaMemcpy(g->in_E, in_E, m * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) s = cuda_status(e);
+  }
+  if (s != PSC_OK) {
+    psc_graph_free(g);
+    return s;
+  }
+  *out = g;
+  return PSC_OK;
+}
+
+int psc_graph_upload_device(const uint64_t* d_off, const uint32_t* d_E, const uint64_t* d_in_off,
+                            const uint32_t* d_in_E, uint64_t n, uint64_t m, psc_graph_t* out) {
+  if (!out || !d_off || (m && !d_E) || n == 0 || n >= 0xFFFFFFFFull) return PSC_ERR_INVALID;
+  if ((d_in_off == nullptr) != (d_in_E == nullptr)) return PSC_ERR_INVALID;
+  psc_graph_s* g = nullptr;
+  PSC_TRY(make_handle(n, m, &g));
+  bool sym = d_in_off == nullptr;
+  int s = alloc_graph_arrays(g, sym);
+  if (s == PSC_OK) {
+    cudaError_t e = cudaMemcpy(g->off, d_off, (n + 1) * 8, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess && m) e = cudaMemcpy(g->E, d_E, m * 4, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess && !sym)
+      e = cudaMemcpy(g->in_off, d_in_off, (n + 1) * 8, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess && !sym && m) e = cudaMemcpy(g->in_E, d_in_E, m * 4, cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) s = cuda_status(e);
+  }
+  if (s != PSC_OK) {
+    psc_graph_free(g);
+    return s;
+  }
+  *out = g;
+  return PSC_OK;
+}
+
+int psc_graph_upload_directed(const uint64_t* off, const uint32_t* E, uint64_t n, uint64_t m,
+                              psc_graph_t* out) {
+  if (!out || !off || (m && !E) || n == 0 || n >= 0xFFFFFFFFull) return PSC_ERR_INVALID;
+  if (off[0] != 0 || off[n] != m) return PSC_ERR_INVALID;
+  psc_graph_s* g = nullptr;
+  PSC_TRY(make_handle(n, m, &g));
+  int s = alloc_graph_arrays(g, false);
+  if (s == PSC_OK) {
+    cudaError_t e = cudaMemcpy(g->off, off, (n + 1) * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && m) e = cudaMemcpy(g->E, E, m * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) s = cuda_status(e);
+  }
+  if (s == PSC_OK) s = build_transpose(g);
+  if (s == PSC_OK) {
+    cudaError_t e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) s = cuda_status(e);
+  }
+  if (s != PSC_OK) {
+    psc_graph_free(g);
+    return s;
+  }
+  *out = g;
+  return PSC_OK;
+}
+
+int psc_graph_download_transpose(psc_graph_t g, uint64_t* in_off, uint32_t* in_E) {
+  if (!g || !in_off || (g->m && !in_E)) return PSC_ERR_INVALID;
+  PSC_CUDA(cudaSetDevice(g->device));
+  PSC_CUDA(cudaStreamSynchronize(g->stream));
+  PSC_CUDA(cudaMemcpy(in_off, g->in_off, (g->n + 1) * 8, cudaMemcpyDeviceToHost));
+  if (g->m) PSC_CUDA(cudaMemcpy(in_E, g->in_E, g->m * 4, cudaMemcpyDeviceToHost));
+  return PSC_OK;
+}
+
+int psc_graph_free(psc_graph_t g) {
+  if (!g) return PSC_OK;
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  for (auto& b : g->bufs)
+    if (b.p) cudaFreeAsync(b.p, g->stream);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  if (g->in_off && g->in_off != g->off) cudaFree(g->in_off);
+  if (g->in_E && g->in_E != g->E) cudaFree(g->in_E);
+  if (g->off) cudaFree(g->off);
+  if (g->E) cudaFree(g->E);
+  if (g->ctr) cudaFree(g->ctr);
+  if (g->hctr) cudaFreeHost(g->hctr);
+  for (auto& p : g->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : g->event_pool) cudaEventDestroy(e);
+  if (g->t0) cudaEventDestroy(g->t0);
+  if (g->t1) cudaEventDestroy(g->t1);
+  if (g->u0) cudaEventDestroy(g->u0);
+  if (g->u1) cudaEventDestroy(g->u1);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+  return PSC_OK;
+}
+
+uint64_t psc_graph_num_vertices(psc_graph_t g) { return g ? g->n : 0; }
+uint64_t psc_graph_num_edges(psc_graph_t g) { return g ? g->m : 0; }
+
+int psc_last_stats(psc_graph_t g, psc_stats_t* out) {
+  if (!g || !out) return PSC_ERR_INVALID;
+  *out = g->stats;
+  return PSC_OK;
+}
+
+int psc_set_profiling(psc_graph_t g, int on) {
+  if (!g) return PSC_ERR_INVALID;
+  g->profiling = on != 0;
+  return PSC_OK;
+}
+
+int psc_profile_count(void) { return F_COUNT; }
+
+int psc_profile_get(psc_graph_t g, int k, const char** name, uint64_t* launches, double* ms,
+                    double* bytes) {
+  if (!g || k < 0 || k >= F_COUNT) return PSC_ERR_INVALID;
+  if (name) *name = kFamilyName[k];
+  if (launches) *launches = g->prof[k].launches;
+  if (ms) *ms = g->prof[k].ms;
+  if (bytes) *bytes = g->prof[k].bytes;
+  return PSC_OK;
+}
+
+int psc_profile_reset(psc_graph_t g) {
+  if (!g) return PSC_ERR_INVALID;
+  for (auto& p : g->prof) p = ProfEntry{};
+  return PSC_OK;
+}
+
+const char* psc_strerror(int s) {
+  switch (s) {
+    case PSC_OK: return "ok";
+    case PSC_ERR_INVALID: return "invalid argument";
+    case PSC_ERR_OOM: return "device out of memory";
+    case PSC_ERR_CUDA: return cudaGetErrorString(g_last_cuda);
+    case PSC_ERR_ITER_LIMIT: return "round loop exceeded its iteration bound";
+    case PSC_ERR_TABLE_FULL: return "label table could not grow";
+    case PSC_ERR_NO_DEVICE: return "no usable CUDA device";
+    case PSC_ERR_CAPACITY: return "output buffer too small";
+    default: return "unknown status";
+  }
+}
+
+int psc_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return PSC_ERR_INVALID;
+  *ptr = nullptr;
+  PSC_CUDA(cudaMallocHost(ptr, bytes ? bytes : 1));
+  return PSC_OK;
+}
+
+int psc_host_free(void* ptr) {
+  if (ptr) PSC_CUDA(cudaFreeHost(ptr));
+  return PSC_OK;
+}
+
+int psc_device_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return PSC_ERR_INVALID;
+  *ptr = nullptr;
+  PSC_CUDA(cudaMalloc(ptr, bytes ? bytes : 1));
+  return PSC_OK;
+}
+
+int psc_device_free(void* ptr) {
+  if (ptr) PSC_CUDA(cudaFree(ptr));
+  return PSC_OK;
+}
+
+int psc_copy(void* dst, const void* src, size_t bytes) {
+  if ((!dst || !src) && bytes) return PSC_ERR_INVALID;
+  if (bytes) PSC_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault));
+  return PSC_OK;
+}
+
+int psc_timer_start(psc_graph_t g) {
+  if (!g) return PSC_ERR_INVALID;
+  PSC_CUDA(cudaSetDevice(g->device));
+  PSC_CUDA(cudaEventRecord(g->u0, g->stream));
+  return PSC_OK;
+}
+
+int psc_timer_stop(psc_graph_t g, double* ms) {
+  if (!g || !ms) return PSC_ERR_INVALID;
+  PSC_CUDA(cudaEventRecord(g->u1, g->stream));
+  PSC_CUDA(cudaEventSynchronize(g->u1));
+  float f = 0;
+  PSC_CUDA(cudaEventElapsedTime(&f, g->u0, g->u1));
+  *ms = f;
+  return PSC_OK;
+}
+
+int psc_set_device(int device) {
+  PSC_CUDA(cudaSetDevice(device));
+  return PSC_OK;
+}
+
+int psc_device_count(void) {
+  int c = 0;
+  if (cudaGetDeviceCount(&c) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return c;
+}
+
+const char* psc_version(void) { return "psc-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,250 @@
+"""Python-side graph objects over the native libraries.
+
+HostGraph   — CSR + transpose in numpy arrays (the reference's struct Graph,
+              src/graph.hpp:35-43), built by libpsc_host.so's seeded
+              generators or read from GBBS .bin files.
+DeviceGraph — a psc_graph_t handle: the same graph resident in HBM, with the
+              SCC / reach / connectivity / LE-list / BFS calls of
+              libpsc_cuda.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import Params, Stats, check
+
+
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class HostGraph:
+    n: int
+    m: int
+    off: np.ndarray              # u64[n+1]
+    E: np.ndarray                # u32[m]
+    in_off: np.ndarray | None = None
+    in_E: np.ndarray | None = None
+    symmetric: bool = False
+
+    # -- construction through libpsc_host.so -------------------------------
+    @staticmethod
+    def _adopt(h: int, what: str) -> "HostGraph":
+        lib = _lib.host()
+        if not h:
+            raise RuntimeError(f"{what}: {lib.psc_host_last_error().decode()}")
+        try:
+            n = lib.psc_hgraph_n(h)
+            m = lib.psc_hgraph_m(h)
+            off = np.ctypeslib.as_array(C.cast(lib.psc_hgraph_off(h), C.POINTER(C.c_uint64)),
+                                        shape=(n + 1,)).copy()
+            E = (np.ctypeslib.as_array(C.cast(lib.psc_hgraph_E(h), C.POINTER(C.c_uint32)),
+                                       shape=(m,)).copy() if m else np.zeros(0, np.uint32))
+            g = HostGraph(int(n), int(m), off, E)
+            ip = lib.psc_hgraph_in_off(h)
+            if ip:
+                g.in_off = np.ctypeslib.as_array(C.cast(ip, C.POINTER(C.c_uint64)),
+                                                 shape=(n + 1,)).copy()
+                g.in_E = (np.ctypeslib.as_array(C.cast(lib.psc_hgraph_in_E(h),
+                                                       C.POINTER(C.c_uint32)), shape=(m,)).copy()
+                          if m else np.zeros(0, np.uint32))
+            return g
+        finally:
+            lib.psc_hgraph_free(h)
+
+    def _handle(self) -> int:
+        lib = _lib.host()
+        h = lib.psc_hgraph_from_csr(self.n, self.m, _ptr(self.off), _ptr(self.E))
+        if not h:
+            raise RuntimeError(lib.psc_host_last_error().decode())
+        return h
+
+    @staticmethod
+    def rmat(log2n: int, draws: int, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1) -> "HostGraph":
+        g = HostGraph._adopt(_lib.host().psc_hgraph_rmat(log2n, draws, a, b, c, seed), "rmat")
+        return g.with_transpose()
+
+    @staticmethod
+    def knn(npts: int, k: int = 5, seed: int = 2) -> "HostGraph":
+        return HostGraph._adopt(_lib.host().psc_hgraph_knn(npts, k, seed), "knn").with_transpose()
+
+    @staticmethod
+    def grid(rows: int, cols: int, p_bidir: float = 0.3, seed: int = 2) -> "HostGraph":
+        return HostGraph._adopt(_lib.host().psc_hgraph_grid(rows, cols, p_bidir, seed),
+                                "grid").with_transpose()
+
+    @staticmethod
+    def from_edges(n: int, src, dst, drop_self: bool = True) -> "HostGraph":
+        src = np.ascontiguousarray(src, dtype=np.uint32)
+        dst = np.ascontiguousarray(dst, dtype=np.uint32)
+        h = _lib.host().psc_hgraph_from_edges(n, len(src), _ptr(src), _ptr(dst), int(drop_self))
+        return HostGraph._adopt(h, "from_edges").with_transpose()
+
+    @staticmethod
+    def read_bin(path: str, large: bool = False) -> "HostGraph":
+        lib = _lib.host()
+        h = (lib.psc_hgraph_read_large if large else lib.psc_hgraph_read_bin)(str(path).encode())
+        g = HostGraph._adopt(h, "read_bin")
+        return g if g.in_off is not None else g.with_transpose()
+
+    def write_bin(self, path: str) -> None:
+        lib = _lib.host()
+        h = self._handle()
+        try:
+            if lib.psc_hgraph_write_bin(h, str(path).encode()) != 0:
+                raise RuntimeError(lib.psc_host_last_error().decode())
+        finally:
+            lib.psc_hgraph_free(h)
+
+    def with_transpose(self) -> "HostGraph":
+        if self.in_off is not None:
+            return self
+        lib = _lib.host()
+        h = self._handle()
+        try:
+            if lib.psc_hgraph_build_transpose(h) != 0:
+                raise RuntimeError(lib.psc_host_last_error().decode())
+            n, m = self.n, self.m
+            self.in_off = np.ctypeslib.as_array(C.cast(lib.psc_hgraph_in_off(h),
+                                                       C.POINTER(C.c_uint64)), shape=(n + 1,)).copy()
+            self.in_E = (np.ctypeslib.as_array(C.cast(lib.psc_hgraph_in_E(h), C.POINTER(C.c_uint32)),
+                                               shape=(m,)).copy() if m else np.zeros(0, np.uint32))
+        finally:
+            lib.psc_hgraph_free(h)
+        return self
+
+    def symmetrize(self) -> "HostGraph":
+        lib = _lib.host()
+        h = self._handle()
+        try:
+            s = lib.psc_hgraph_symmetrize(h)
+        finally:
+            lib.psc_hgraph_free(h)
+        g = HostGraph._adopt(s, "symmetrize")
+        g.symmetric = True
+        g.in_off, g.in_E = g.off, g.E
+        return g
+
+    def edge_list(self) -> tuple[np.ndarray, np.ndarray]:
+        src = np.repeat(np.arange(self.n, dtype=np.uint32), np.diff(self.off).astype(np.int64))
+        return src, self.E
+
+
+def random_permutation(n: int, seed: int) -> np.ndarray:
+    """perm[i] = Feistel bijection of i on [0, n) (stands in for
+    parlay::random_permutation, src/LeList.hpp:67)."""
+    out = np.empty(n, dtype=np.uint32)
+    _lib.host().psc_random_permutation(n, seed, _ptr(out))
+    return out
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    _lib.cuda().psc_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, "lambda_" if k == "lambda" else k, v)
+    return p
+
+
+class DeviceGraph:
+    """A graph resident on the current CUDA device (psc_graph_t)."""
+
+    def __init__(self, g: HostGraph | None = None, *, handle: int | None = None):
+        self._lib = _lib.cuda()
+        if handle is not None:
+            self.h = handle
+        else:
+            assert g is not None
+            h = C.c_void_p()
+            if g.symmetric:
+                st = self._lib.psc_graph_upload(_ptr(g.off), _ptr(g.E), None, None, g.n, g.m,
+                                                C.byref(h))
+            else:
+                gt = g.with_transpose()
+                st = self._lib.psc_graph_upload(_ptr(gt.off), _ptr(gt.E), _ptr(gt.in_off),
+                                                _ptr(gt.in_E), g.n, g.m, C.byref(h))
+            check(st, "psc_graph_upload")
+            self.h = h.value
+        self.n = int(self._lib.psc_graph_num_vertices(self.h))
+        self.m = int(self._lib.psc_graph_num_edges(self.h))
+
+    @staticmethod
+    def directed(off: np.ndarray, E: np.ndarray) -> "DeviceGraph":
+        """Upload a CSR and build its transpose on the device."""
+        lib = _lib.cuda()
+        off = np.ascontiguousarray(off, dtype=np.uint64)
+        E = np.ascontiguousarray(E, dtype=np.uint32)
+        h = C.c_void_p()
+        check(lib.psc_graph_upload_directed(_ptr(off), _ptr(E), len(off) - 1, len(E), C.byref(h)),
+              "psc_graph_upload_directed")
+        return DeviceGraph(handle=h.value)
+
+    def free(self) -> None:
+        if getattr(self, "h", None):
+            self._lib.psc_graph_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.free()
+
+    def transpose(self) -> tuple[np.ndarray, np.ndarray]:
+        in_off = np.empty(self.n + 1, np.uint64)
+        in_E = np.empty(max(self.m, 1), np.uint32)
+        check(self._lib.psc_graph_download_transpose(self.h, _ptr(in_off), _ptr(in_E)),
+              "psc_graph_download_transpose")
+        return in_off, in_E[: self.m]
+
+    def scc(self, params: Params | None = None, out: np.ndarray | None = None) -> np.ndarray:
+        p = params or default_params()
+        labels = out if out is not None else np.empty(self.n, np.uint64)
+        check(self._lib.psc_scc(self.h, C.byref(p), _ptr(labels)), "psc_scc")
+        return labels
+
+    def scc_device(self, d_labels: int, params: Params | None = None) -> None:
+        p = params or default_params()
+        check(self._lib.psc_scc_device(self.h, C.byref(p), d_labels), "psc_scc_device")
+
+    def reach(self, src: int, backward: bool = False, local: bool = True,
+              tau: int = 512) -> np.ndarray:
+        dst = np.empty(self.n, np.uint8)
+        r = C.c_uint32()
+        check(self._lib.psc_reach(self.h, src, int(backward), int(local), tau, _ptr(dst),
+                                  C.byref(r)), "psc_reach")
+        self.last_rounds = r.value
+        return dst
+
+    def stats(self) -> Stats:
+        s = Stats()
+        check(self._lib.psc_last_stats(self.h, C.byref(s)), "psc_last_stats")
+        return s
+
+    def set_profiling(self, on: bool) -> None:
+        check(self._lib.psc_set_profiling(self.h, int(on)), "psc_set_profiling")
+
+    def profile(self) -> dict[str, dict]:
+        out = {}
+        for k in range(self._lib.psc_profile_count()):
+            name = C.c_char_p()
+            la, ms, by = C.c_uint64(), C.c_double(), C.c_double()
+            check(self._lib.psc_profile_get(self.h, k, C.byref(name), C.byref(la), C.byref(ms),
+                                            C.byref(by)), "psc_profile_get")
+            out[name.value.decode()] = {"launches": la.value, "ms": ms.value, "bytes": by.value}
+        return out
+
+    def profile_reset(self) -> None:
+        check(self._lib.psc_profile_reset(self.h), "psc_profile_reset")

@@ -76,13 +76,15 @@ def test_scc_symmetric_upload():
 
 
 def test_scc_table_growth_path():
-    """A single giant batch on a dense graph forces the (v, pivot) table to
-    grow and sub-rounds to be re-run; labels must not change."""
-    g = generated("rmat", 12, 11)
+    """A batch of ~100 pivots on a long chain: every pivot reaches the rest of
+    the chain inside one subproblem, so the (v, pivot) closure (~6*10^4 pairs)
+    outgrows the first table many times over.  Labels must not change."""
+    n = 1200
+    g = psc.HostGraph.from_edges(n, np.arange(n - 1), np.arange(1, n))
     with psc.DeviceGraph(g) as dg:
-        lab = dg.scc(psc.default_params(seed=2, beta=1000.0))
+        lab = dg.scc(psc.default_params(seed=2, beta=100.0))
         assert dg.stats().table_grows > 0
-    ref = O.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=2, beta=1000.0)
+    ref = O.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=2, beta=100.0)
     assert np.array_equal(lab, ref)
 
 

@@ -94,6 +94,9 @@ typedef struct {
   uint64_t subrounds;       /* multi-search sub-rounds, both directions */
   uint64_t table_grows;     /* label-table rehashes */
   uint64_t kernel_launches; /* kernels launched by the call */
+  /* SCC phase times in ms (the breakdown of src/scc.hpp:94-114):
+   * [0] init/trim, [1] first round, [2] multi-search, [3] table resizing */
+  double phase_ms[4];
 } psc_stats_t;
 int psc_last_stats(psc_graph_t g, psc_stats_t* out);
 

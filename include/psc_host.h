@@ -6,6 +6,7 @@
  *
  * Reference interfaces replaced:
  *   psc_hgraph_read_bin / write_bin  <- read_binary, src/graph.hpp:120-185
+ *   psc_hgraph_read_adj              <- read_pbbs, src/graph.hpp:73-118
  *   psc_hgraph_read_large            <- read_large_graph, src/graph.hpp:279-315
  *   psc_hgraph_build_transpose       <- make_directed, src/graph.hpp:222-245
  *   psc_hgraph_symmetrize            <- make_symmetric, src/graph.hpp:187-220
@@ -56,6 +57,9 @@ psc_hgraph_t psc_hgraph_from_csr(uint64_t n, uint64_t m, const uint64_t* off, co
 /* GBBS binary format: u64 n, u64 m, u64 sizes, u64 off[n+1], u32 E[m]. */
 psc_hgraph_t psc_hgraph_read_bin(const char* path);
 int psc_hgraph_write_bin(psc_hgraph_t g, const char* path);
+/* PBBS text format "AdjacencyGraph n m off[0..n) E[0..m)" (read_pbbs,
+ * src/graph.hpp:73-118). */
+psc_hgraph_t psc_hgraph_read_adj(const char* path);
 /* Two CSRs back to back (forward then transpose), as read_large_graph. */
 psc_hgraph_t psc_hgraph_read_large(const char* path);
 

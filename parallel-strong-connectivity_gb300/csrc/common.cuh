@@ -104,6 +104,8 @@ struct psc_graph_s {
   std::vector<cudaEvent_t> event_pool;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   cudaEvent_t u0 = nullptr, u1 = nullptr;  // caller timer (psc_timer_*)
+  cudaEvent_t ph[4] = {nullptr, nullptr, nullptr, nullptr};  // SCC phase marks
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> grow_events;  // table resizes
 };
 
 namespace psc {
@@ -173,6 +175,8 @@ int zero_counters(psc_graph_s* g);
 void prof_begin(psc_graph_s* g, int fam, cudaEvent_t* a);
 void prof_end(psc_graph_s* g, int fam, cudaEvent_t a, double bytes);
 int prof_flush(psc_graph_s* g);
+cudaEvent_t take_event(psc_graph_s* g);
+void give_event(psc_graph_s* g, cudaEvent_t e);
 
 struct ProfScope {
   psc_graph_s* g;

@@ -76,7 +76,7 @@ int read_counters(psc_graph_s* g) {
   return PSC_OK;
 }
 
-static cudaEvent_t pool_event(psc_graph_s* g) {
+cudaEvent_t take_event(psc_graph_s* g) {
   if (!g->event_pool.empty()) {
     cudaEvent_t e = g->event_pool.back();
     g->event_pool.pop_back();
@@ -87,15 +87,17 @@ static cudaEvent_t pool_event(psc_graph_s* g) {
   return e;
 }
 
+void give_event(psc_graph_s* g, cudaEvent_t e) { g->event_pool.push_back(e); }
+
 void prof_begin(psc_graph_s* g, int, cudaEvent_t* a) {
   if (!g->profiling) return;
-  *a = pool_event(g);
+  *a = take_event(g);
   cudaEventRecord(*a, g->stream);
 }
 
 void prof_end(psc_graph_s* g, int fam, cudaEvent_t a, double bytes) {
   if (!g->profiling || !a) return;
-  cudaEvent_t b = pool_event(g);
+  cudaEvent_t b = take_event(g);
   cudaEventRecord(b, g->stream);
   g->pending.push_back(PendingEvent{fam, a, b, bytes});
   if (g->pending.size() > 4096) prof_flush(g);
@@ -163,7 +165,9 @@ static int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
       (e = cudaMalloc(&g->ctr, sizeof(Counters))) != cudaSuccess ||
       (e = cudaMallocHost(&g->hctr, sizeof(Counters))) != cudaSuccess ||
       (e = cudaEventCreate(&g->t0)) != cudaSuccess || (e = cudaEventCreate(&g->t1)) != cudaSuccess ||
-      (e = cudaEventCreate(&g->u0)) != cudaSuccess || (e = cudaEventCreate(&g->u1)) != cudaSuccess) {
+      (e = cudaEventCreate(&g->u0)) != cudaSuccess || (e = cudaEventCreate(&g->u1)) != cudaSuccess ||
+      (e = cudaEventCreate(&g->ph[0])) != cudaSuccess || (e = cudaEventCreate(&g->ph[1])) != cudaSuccess ||
+      (e = cudaEventCreate(&g->ph[2])) != cudaSuccess || (e = cudaEventCreate(&g->ph[3])) != cudaSuccess) {
     psc_graph_free(g);
     return cuda_status(e);
   }
@@ -312,6 +316,12 @@ int psc_graph_free(psc_graph_t g) {
   for (auto e : g->event_pool) cudaEventDestroy(e);
   if (g->t0) cudaEventDestroy(g->t0);
   if (g->t1) cudaEventDestroy(g->t1);
+  for (auto e : g->ph)
+    if (e) cudaEventDestroy(e);
+  for (auto& pr : g->grow_events) {
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
   if (g->u0) cudaEventDestroy(g->u0);
   if (g->u1) cudaEventDestroy(g->u1);
   if (g->stream) cudaStreamDestroy(g->stream);

@@ -408,6 +408,56 @@ psc_hgraph_t psc_hgraph_read_bin(const char* path) {
   return g;
 }
 
+psc_hgraph_t psc_hgraph_read_adj(const char* path) {
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    set_err(std::string("Cannot open file ") + path);
+    return nullptr;
+  }
+  std::string text;
+  {
+    char buf[1 << 16];
+    size_t k;
+    while ((k = fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, k);
+    fclose(f);
+  }
+  // whitespace-separated words (src/graph.hpp:88-105)
+  std::vector<const char*> words;
+  for (size_t i = 0; i < text.size();) {
+    while (i < text.size() && (text[i] == ' ' || text[i] == '\n' || text[i] == '\r' ||
+                               text[i] == '\t' || text[i] == 0))
+      text[i++] = 0;
+    if (i < text.size()) words.push_back(&text[i]);
+    while (i < text.size() && !(text[i] == ' ' || text[i] == '\n' || text[i] == '\r' ||
+                                text[i] == '\t' || text[i] == 0))
+      i++;
+  }
+  if (words.size() < 3) {
+    set_err(std::string("Bad data in ") + path);
+    return nullptr;
+  }
+  uint64_t n = strtoull(words[1], nullptr, 10), m = strtoull(words[2], nullptr, 10);
+  if (words.size() < 3 + n + m || n >= 0xFFFFFFFFull) {
+    set_err(std::string("Bad data in ") + path);
+    return nullptr;
+  }
+  auto* g = new psc_hgraph_s();
+  g->n = n;
+  g->m = m;
+  g->off.resize(n + 1);
+  g->E.resize(m);
+  for (uint64_t i = 0; i < n; i++) g->off[i] = strtoull(words[3 + i], nullptr, 10);
+  g->off[n] = m;
+  for (uint64_t j = 0; j < m; j++) g->E[j] = (uint32_t)strtoull(words[3 + n + j], nullptr, 10);
+  for (uint64_t i = 0; i < n; i++)
+    if (g->off[i + 1] < g->off[i]) {
+      delete g;
+      set_err(std::string("Bad offsets in ") + path);
+      return nullptr;
+    }
+  return g;
+}
+
 psc_hgraph_t psc_hgraph_read_large(const char* path) {
   FILE* f = fopen(path, "rb");
   if (!f) {

@@ -273,6 +273,8 @@ struct MsResult {
 
 // Rehash the table in slot tslot into a new table of capacity cap2.
 static int ms_grow(psc_graph_s* g, int tslot, uint64_t cap, uint64_t cap2) {
+  cudaEvent_t ea = take_event(g), eb = take_event(g);
+  PSC_CUDA(cudaEventRecord(ea, g->stream));
   unsigned long long *T, *T2;
   T = (unsigned long long*)g->bufs[tslot].p;
   PSC_TRY(ensure_t(g, B_TS, cap2, &T2));
@@ -285,6 +287,8 @@ static int ms_grow(psc_graph_s* g, int tslot, uint64_t cap, uint64_t cap2) {
   PSC_CUDA(cudaGetLastError());
   swap_bufs(g, tslot, B_TS);
   g->stats.table_grows++;
+  PSC_CUDA(cudaEventRecord(eb, g->stream));
+  g->grow_events.emplace_back(ea, eb);
   return PSC_OK;
 }
 
@@ -372,7 +376,35 @@ static int ms_run(psc_graph_s* g, bool backward, const uint32_t* front, uint64_t
   return PSC_OK;
 }
 
+static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p);
+
 int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
+  for (auto& pr : g->grow_events) {
+    give_event(g, pr.first);
+    give_event(g, pr.second);
+  }
+  g->grow_events.clear();
+  PSC_CUDA(cudaEventRecord(g->ph[0], g->stream));
+  PSC_TRY(scc_phases(g, labels, p));
+  PSC_CUDA(cudaEventSynchronize(g->ph[3]));
+  float a = 0, b = 0, c = 0;
+  PSC_CUDA(cudaEventElapsedTime(&a, g->ph[0], g->ph[1]));
+  PSC_CUDA(cudaEventElapsedTime(&b, g->ph[1], g->ph[2]));
+  PSC_CUDA(cudaEventElapsedTime(&c, g->ph[2], g->ph[3]));
+  double grow = 0;
+  for (auto& pr : g->grow_events) {
+    float x = 0;
+    PSC_CUDA(cudaEventElapsedTime(&x, pr.first, pr.second));
+    grow += x;
+  }
+  g->stats.phase_ms[0] = a;
+  g->stats.phase_ms[1] = b;
+  g->stats.phase_ms[2] = c - grow;
+  g->stats.phase_ms[3] = grow;
+  return PSC_OK;
+}
+
+static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
   const uint64_t n = g->n;
   const unsigned tb = 256;
   uint32_t *P, *nz, *centers, *front, *vf, *vb;
@@ -388,6 +420,7 @@ int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
     k_perm_gather<<<grid_for(g, np, tb), tb, 0, g->stream>>>(nz, np, key, P);
   }
   uint64_t label_offset = n_zeros + 1;
+  PSC_CUDA(cudaEventRecord(g->ph[1], g->stream));
   if (np > 0) {
     // first pivot (scc.hpp:316-350)
     uint32_t src = 0;
@@ -409,6 +442,7 @@ int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
     uint64_t nc = 0;
     PSC_TRY(scan_emit(g, np, NotDoneAt{P, labels, 0}, CopyAt{P, centers, 0}, &nc));
     label_offset++;
+    PSC_CUDA(cudaEventRecord(g->ph[2], g->stream));
 
     // prefix-doubling batches (scc.hpp:365-473)
     PSC_TRY(ensure_t(g, B_FRONT, np + 1, &front));
@@ -453,6 +487,8 @@ int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
       in_ne = rb.ne;
     }
   }
+  if (np == 0) PSC_CUDA(cudaEventRecord(g->ph[2], g->stream));
+  PSC_CUDA(cudaEventRecord(g->ph[3], g->stream));
   {
     ProfScope ps(g, F_FINALISE);
     ps.bytes = 16.0 * n;

@@ -73,6 +73,9 @@ def build_all(force: bool = False) -> None:
         b = ex.submit(build_host, force)
         a.result()
         b.result()
+    from . import _drivers
+
+    _drivers.build_drivers(force)
 
 
 if __name__ == "__main__":

@@ -54,6 +54,7 @@ class Stats(C.Structure):
         ("subrounds", C.c_uint64),
         ("table_grows", C.c_uint64),
         ("kernel_launches", C.c_uint64),
+        ("phase_ms", C.c_double * 4),
     ]
 
 
@@ -104,6 +105,7 @@ HOST_SIGNATURES = {
     "psc_hgraph_read_bin": (P, [C.c_char_p]),
     "psc_hgraph_write_bin": (I32, [P, C.c_char_p]),
     "psc_hgraph_read_large": (P, [C.c_char_p]),
+    "psc_hgraph_read_adj": (P, [C.c_char_p]),
     "psc_hgraph_build_transpose": (I32, [P]),
     "psc_hgraph_symmetrize": (P, [P]),
     "psc_hgraph_n": (U64, [P]),

@@ -131,3 +131,18 @@ def test_bin_round_trip(tmp_path):
         psc.HostGraph.read_bin(bad)
     with pytest.raises(RuntimeError):
         psc.HostGraph.read_bin(tmp_path / "missing.bin")
+
+
+def test_adj_reader(tmp_path):
+    g = psc.HostGraph.rmat(8, 1 << 10, seed=5)
+    p = tmp_path / "g.adj"
+    lines = ["AdjacencyGraph", str(g.n), str(g.m)] + [str(x) for x in g.off[:-1]] + \
+        [str(x) for x in g.E]
+    p.write_text("\n".join(lines) + "\n")
+    lib = psc.host()
+    h = lib.psc_hgraph_read_adj(str(p).encode())
+    assert h
+    r = psc.HostGraph._adopt(h, "adj")
+    assert np.array_equal(r.off, g.off) and np.array_equal(r.E, g.E)
+    (tmp_path / "bad.adj").write_text("AdjacencyGraph\n5\n")
+    assert not lib.psc_hgraph_read_adj(str(tmp_path / "bad.adj").encode())

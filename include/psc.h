@@ -32,7 +32,8 @@ enum {
   PSC_ERR_ITER_LIMIT = 4, /* a round loop exceeded its bound */
   PSC_ERR_TABLE_FULL = 5, /* label table could not grow further */
   PSC_ERR_NO_DEVICE = 6,  /* no usable CUDA device */
-  PSC_ERR_CAPACITY = 7    /* caller buffer too small (see the function) */
+  PSC_ERR_CAPACITY = 7,   /* caller buffer too small (see the function) */
+  PSC_ERR_TOO_LARGE = 8   /* graph exceeds psc_reach_noalloc's fixed scratch */
 };
 
 typedef struct psc_graph_s* psc_graph_t;
@@ -84,6 +85,35 @@ int psc_scc_device(psc_graph_t g, const psc_params_t* p, uint64_t* d_labels);
  * REACH::swap_graph).  Returns rounds via *rounds if non-NULL. */
 int psc_reach(psc_graph_t g, uint32_t src, int dir, int local, uint32_t tau, uint8_t* dst_out,
               uint32_t* rounds);
+
+/* psc_reach without any memory allocation.  No counterpart in the reference.
+ *
+ * For callers that may not allocate device memory themselves: engines that
+ * own the GPU's memory budget and hand out every buffer through their own
+ * allocator, and latency-critical code that cannot afford the device-wide
+ * synchronisation cudaMalloc / cudaFree may imply.  The caller passes device
+ * pointers to the graph (d_in_off / d_in_E may be NULL for a symmetric graph)
+ * and to the output d_dst (u8[n], 1 = reachable from src; dir 0 = forward,
+ * 1 = backward), and the stream to run on (NULL = the legacy default stream).
+ * The call allocates nothing: it uses no psc_graph_t, no cudaMalloc/cudaFree
+ * and no allocating library routine.  Its scratch (visited and frontier
+ * bitmaps, two frontier queues, the heavy list and the round counters) is one
+ * file-scope __device__ array sized for PSC_NOALLOC_MAX_VERTICES vertices,
+ * about 26 MB, which every GPU that loads the library holds until the
+ * process exits.  Larger graphs are rejected with PSC_ERR_TOO_LARGE before
+ * any device work.
+ *
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before
+ * any stream capture.  All calls share the one array, which keeps the previous
+ * call's contents (each call clears what must start at zero): calls that
+ * overlap on the GPU — on different streams or from different host threads —
+ * race and give wrong results.  Host-synchronous like psc_reach; *rounds (if
+ * non-NULL) receives the number of frontier rounds. */
+#define PSC_NOALLOC_MAX_VERTICES (1u << 21)
+int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E, const uint64_t* d_in_off,
+                      const uint32_t* d_in_E, uint64_t n, uint64_t m, uint32_t src, int dir,
+                      uint8_t* d_dst, void* stream, uint32_t* rounds);
 
 /* Per-call statistics of the last psc_scc / psc_reach / psc_cc / psc_lelist
  * on this handle. */

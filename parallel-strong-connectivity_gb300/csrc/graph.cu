@@ -372,6 +372,8 @@ const char* psc_strerror(int s) {
     case PSC_ERR_TABLE_FULL: return "label table could not grow";
     case PSC_ERR_NO_DEVICE: return "no usable CUDA device";
     case PSC_ERR_CAPACITY: return "output buffer too small";
+    case PSC_ERR_TOO_LARGE:
+      return "graph exceeds the fixed scratch of psc_reach_noalloc (PSC_NOALLOC_MAX_VERTICES)";
     default: return "unknown status";
   }
 }

@@ -18,6 +18,8 @@
 // VGC (local search, reach.hpp:114-171) runs each low-degree frontier vertex
 // as a warp-local BFS in shared memory that claims up to tau vertices in the
 // same round before spilling the rest to the global frontier.
+#include <mutex>
+
 #include "common.cuh"
 #include "engines.cuh"
 
@@ -288,4 +290,145 @@ extern "C" int psc_reach(psc_graph_t g, uint32_t src, int dir, int local, uint32
   g->stats.reach_rounds = r;
   if (rounds) *rounds = r;
   return call_end(g);
+}
+
+// ---------------------------------------------------------------------------
+// psc_reach_noalloc: the same reach kernels with their scratch in one
+// file-scope device array instead of allocated buffers.
+// ---------------------------------------------------------------------------
+namespace psc {
+
+constexpr uint64_t kNaMaxN = PSC_NOALLOC_MAX_VERTICES;
+constexpr uint64_t kNaWords = kNaMaxN / 32;
+// Region sizes are multiples of 64 u32 (256 bytes) so every region, and the
+// Counters block at the end, starts 256-byte aligned.
+constexpr size_t kNaBitmap = kNaWords + 64;
+constexpr size_t kNaQueue = kNaMaxN + 64;
+constexpr size_t kNaVis = 0;
+constexpr size_t kNaFa = kNaVis + kNaBitmap;
+constexpr size_t kNaFb = kNaFa + kNaBitmap;
+constexpr size_t kNaQa = kNaFb + kNaBitmap;
+constexpr size_t kNaQb = kNaQa + kNaQueue;
+constexpr size_t kNaHeavy = kNaQb + kNaQueue;
+constexpr size_t kNaCtr = kNaHeavy + kNaQueue;
+constexpr size_t kNaTotal = kNaCtr + 64;
+static_assert(sizeof(Counters) <= 64 * sizeof(uint32_t), "counters fit their region");
+static_assert(kNaCtr % 64 == 0, "256-byte aligned counters");
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaTotal];
+
+struct NoAllocDevice {
+  uint32_t* scratch = nullptr;
+  int num_sms = 0;
+  bool ready = false;
+};
+constexpr int kNaMaxDevices = 64;
+static NoAllocDevice g_na_dev[kNaMaxDevices];
+static std::mutex g_na_mu;
+
+// Once per device, with that device current: the array's device address.
+static int noalloc_setup(int dev, NoAllocDevice* out) {
+  if (dev < 0 || dev >= kNaMaxDevices) return PSC_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(g_na_mu);
+  NoAllocDevice& d = g_na_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e);
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_status(e);
+    d.scratch = (uint32_t*)p;
+    d.num_sms = sms;
+    d.ready = true;
+  }
+  *out = d;
+  return PSC_OK;
+}
+
+static unsigned na_grid(int sms, uint64_t items, unsigned block) {
+  uint64_t want = (items + block - 1) / block;
+  uint64_t cap = (uint64_t)sms * 16;
+  if (want < 1) want = 1;
+  if (want > cap) want = cap;
+  return (unsigned)want;
+}
+
+}  // namespace psc
+
+extern "C" int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E,
+                                 const uint64_t* d_in_off, const uint32_t* d_in_E, uint64_t n,
+                                 uint64_t m, uint32_t src, int dir, uint8_t* d_dst, void* stream,
+                                 uint32_t* rounds) {
+  if (n > kNaMaxN) return PSC_ERR_TOO_LARGE;
+  if (!d_off || (m && !d_E) || !d_dst || n == 0 || src >= n || (dir != 0 && dir != 1))
+    return PSC_ERR_INVALID;
+  if ((d_in_off == nullptr) != (d_in_E == nullptr)) return PSC_ERR_INVALID;
+  if (!d_in_off) {  // symmetric: the transpose is the graph itself
+    d_in_off = d_off;
+    d_in_E = d_E;
+  }
+  int dev = 0;
+  PSC_CUDA(cudaGetDevice(&dev));
+  NoAllocDevice nd;
+  PSC_TRY(noalloc_setup(dev, &nd));
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool backward = dir == 1;
+  const uint64_t* A_off = backward ? d_in_off : d_off;
+  const uint32_t* A_E = backward ? d_in_E : d_E;
+  const uint64_t* B_off = backward ? d_off : d_in_off;
+  const uint32_t* B_E = backward ? d_E : d_in_E;
+  const uint64_t nwords = (n + 31) / 32;
+  uint32_t* vis = nd.scratch + kNaVis;
+  uint32_t* fa = nd.scratch + kNaFa;
+  uint32_t* fb = nd.scratch + kNaFb;
+  uint32_t* qa = nd.scratch + kNaQa;
+  uint32_t* qb = nd.scratch + kNaQb;
+  uint32_t* heavy = nd.scratch + kNaHeavy;
+  Counters* ctr = (Counters*)(nd.scratch + kNaCtr);
+  Counters hc;  // host copy of the counters (stack memory)
+
+  // the array keeps the previous call's contents: clear the visited bitmap
+  PSC_CUDA(cudaMemsetAsync(vis, 0, nwords * 4, s));
+  k_reach_init<<<1, 1, 0, s>>>(vis, qa, src);
+  const uint64_t threshold = m / 20;
+  uint64_t nf = 1, nf_edges = 0;
+  bool pull = false;
+  uint32_t r = 0;
+  while (nf > 0) {
+    r++;
+    if (r > n + 2) return PSC_ERR_ITER_LIMIT;
+    const bool want_pull = (nf + nf_edges) >= threshold;
+    if (want_pull && !pull) {
+      PSC_CUDA(cudaMemsetAsync(fa, 0, nwords * 4, s));
+      k_queue_to_bitmap<<<na_grid(nd.num_sms, nf, 256), 256, 0, s>>>(qa, nf, fa);
+      pull = true;
+    } else if (!want_pull && pull) {
+      PSC_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), s));
+      k_bitmap_to_queue<<<na_grid(nd.num_sms, nwords, 256), 256, 0, s>>>(fa, nwords, qa, ctr);
+      pull = false;
+    }
+    PSC_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), s));
+    if (!pull) {
+      k_reach_push<kReachBlock><<<na_grid(nd.num_sms, nf, kReachBlock), kReachBlock, 0, s>>>(
+          A_off, A_E, qa, nf, vis, qb, heavy, ctr);
+      k_reach_heavy<kReachBlock><<<nd.num_sms * 4, kReachBlock, 0, s>>>(A_off, A_E, heavy, ctr,
+                                                                       vis, qb);
+      std::swap(qa, qb);
+    } else {
+      k_reach_pull<kReachBlock><<<na_grid(nd.num_sms, nwords * 32, kReachBlock), kReachBlock, 0, s>>>(
+          B_off, B_E, A_off, fa, vis, fb, n, ctr);
+      std::swap(fa, fb);
+    }
+    PSC_CUDA(cudaGetLastError());
+    PSC_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    PSC_CUDA(cudaStreamSynchronize(s));
+    nf = hc.next;
+    nf_edges = hc.next_edges;
+  }
+  k_bitmap_to_bytes<<<na_grid(nd.num_sms, n, 256), 256, 0, s>>>(vis, n, d_dst);
+  PSC_CUDA(cudaGetLastError());
+  PSC_CUDA(cudaStreamSynchronize(s));
+  if (rounds) *rounds = r;
+  return PSC_OK;
 }

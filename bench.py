@@ -345,10 +345,15 @@ def run_gpu(args, world, rank, local, dist) -> None:
                    "beta": 1.5, "tau": 512, "vgc": True, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (no flush)" if (h2d > 129e6) else "L2-resident",
                    "batches": last.batches, "subrounds": last.subrounds,
-                   "reach_rounds": last.reach_rounds},
+                   "reach_rounds": last.reach_rounds,
+                   "phase_ms": {"trim": last.phase_ms[0], "first_pivot": last.phase_ms[1],
+                                "multi_search": last.phase_ms[2], "table_resize": last.phase_ms[3]}},
         "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / args.steps * 1e3},
         "roofline": roofline,
+        "profile": {k: {"launches": v["launches"] // max(1, args.profile_steps),
+                        "ms": v["ms"] / max(1, args.profile_steps)}
+                    for k, v in prof.items() if v["launches"]},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": launches,

@@ -26,6 +26,7 @@
 namespace psc {
 
 constexpr int kReachBlock = 256;
+constexpr int kVgcQueue = 512;  // VGC queue entries per warp (16 KB per block)
 
 __global__ void k_reach_init(uint32_t* vis, uint32_t* q, uint32_t src) {
   vis[src >> 5] = 1u << (src & 31);
@@ -70,6 +71,111 @@ __global__ void __launch_bounds__(BLOCK)
         next_edges += off[v + 1] - off[v];
       }
     });
+  }
+  scanned = warp_sum(scanned);
+  next_edges = warp_sum(next_edges);
+  if (lane == 0) {
+    if (scanned) atomicAdd(&ctr->edges, scanned);
+    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
+  }
+}
+
+// VGC push round (reach.hpp:114-171): one frontier vertex per warp.  A vertex
+// with 0 < deg < tau starts a local BFS in a shared-memory queue of tq =
+// min(tau, QCAP) entries: the warp expands up to 32 queued vertices per wave
+// with the balanced expansion, claims neighbours on the visited bitmap, and
+// keeps a claimed vertex in the queue while it has room, else spills it to the
+// next global frontier.  Queued vertices with more than tq out-edges, and
+// whatever is left in the queue when it fills, are spilled as well.  Other
+// frontier vertices are expanded directly (heavy ones by the whole grid).
+template <int BLOCK, int QCAP>
+__global__ void __launch_bounds__(BLOCK)
+    k_reach_vgc(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
+                const uint32_t* __restrict__ qin, uint64_t nin, uint32_t* vis, uint32_t* qout,
+                uint32_t* heavy, Counters* ctr, uint32_t tau) {
+  __shared__ WarpExpandSmem sm[BLOCK / 32];
+  __shared__ uint32_t sq[BLOCK / 32][QCAP];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
+  uint32_t* Q = sq[wid];
+  unsigned long long scanned = 0, next_edges = 0;
+  auto emit = [&](bool take, uint32_t v) {
+    unsigned long long pos = warp_append(&ctr->next, take);
+    if (take) {
+      qout[pos] = v;
+      next_edges += off[v + 1] - off[v];
+    }
+  };
+  for (uint64_t i = gw; i < nin; i += nw) {
+    const uint32_t u = qin[i];
+    const uint64_t ub = off[u], ue = off[u + 1];
+    const uint64_t du = ue - ub;
+    if (!(du > 0 && du < tq)) {
+      if (du > kHeavyDeg) {
+        if (lane == 0) heavy[atomicAdd(&ctr->heavy, 1ull)] = u;
+        continue;
+      }
+      if (lane == 0) scanned += du;
+      for (uint64_t b = ub; b < ue; b += 32) {
+        const uint64_t e = b + lane;
+        uint32_t v = 0;
+        bool take = false;
+        if (e < ue) {
+          v = __ldg(&E[e]);
+          take = bit_set(vis, v);
+        }
+        emit(take, v);
+      }
+      continue;
+    }
+    if (lane == 0) Q[0] = u;
+    __syncwarp();
+    uint32_t head = 0, tail = 1;
+    while (head < tail && tail < tq) {
+      const uint32_t wave = min(32u, tail - head);
+      uint64_t beg = 0;
+      uint32_t deg = 0, x = 0;
+      bool spill_self = false;
+      if (lane < wave) {
+        x = Q[head + lane];
+        beg = off[x];
+        uint64_t d = off[x + 1] - beg;
+        if (d > tq) {
+          spill_self = true;
+          d = 0;
+        }
+        deg = (uint32_t)d;
+      }
+      head += wave;
+      __syncwarp();
+      emit(spill_self, x);
+      scanned += deg;
+      warp_expand(sm[wid], beg, deg, [&](bool act, int, uint64_t e) {
+        uint32_t v = 0;
+        bool take = false;
+        if (act) {
+          v = __ldg(&E[e]);
+          take = bit_set(vis, v);
+        }
+        const unsigned mask = __ballot_sync(kFull, take);
+        const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
+        const uint32_t room = tq - tail;
+        const bool local = take && rank < room;
+        if (local) Q[tail + rank] = v;
+        const uint32_t nt = __popc(mask);
+        tail += nt < room ? nt : room;
+        emit(take && !local, v);
+      });
+      __syncwarp();
+    }
+    for (uint32_t b = head; b < tail; b += 32) {
+      const uint32_t k = b + lane;
+      const bool t = k < tail;
+      emit(t, t ? Q[k] : 0u);
+    }
+    __syncwarp();
   }
   scanned = warp_sum(scanned);
   next_edges = warp_sum(next_edges);
@@ -199,9 +305,9 @@ __global__ void k_bitmap_to_queue(const uint32_t* __restrict__ fb, uint64_t nwor
 
 int reach_run(psc_graph_s* g, uint32_t src, bool backward, bool local, uint32_t tau,
               uint32_t pull_div, uint32_t* vis, uint32_t* rounds_out) {
-  (void)local;
-  (void)tau;
   const uint64_t n = g->n, nwords = (n + 31) / 32;
+  // VGC rounds while the frontier is below one vertex per resident warp
+  const uint64_t vgc_limit = (uint64_t)g->num_sms * 64;
   const uint64_t* A_off = backward ? g->in_off : g->off;
   const uint32_t* A_E = backward ? g->in_E : g->E;
   const uint64_t* B_off = backward ? g->off : g->in_off;
@@ -236,9 +342,13 @@ int reach_run(psc_graph_s* g, uint32_t src, bool backward, bool local, uint32_t 
     }
     PSC_TRY(zero_counters(g));
     if (!pull) {
-      {
+      if (local && nf <= vgc_limit) {
+        ProfScope ps(g, F_REACH_VGC);
+        k_reach_vgc<kReachBlock, kVgcQueue>
+            <<<grid_for(g, nf * 32, kReachBlock), kReachBlock, 0, g->stream>>>(
+                A_off, A_E, qa, nf, vis, qb, heavy, g->ctr, tau ? tau : 512);
+      } else {
         ProfScope ps(g, F_REACH_PUSH);
-        ps.bytes = 16.0 * nf + 5.0 * nf_edges;
         k_reach_push<kReachBlock><<<grid_for(g, nf, kReachBlock), kReachBlock, 0, g->stream>>>(
             A_off, A_E, qa, nf, vis, qb, heavy, g->ctr);
       }

@@ -49,6 +49,7 @@ enum Family : int {
 extern const char* const kFamilyName[F_COUNT];
 
 // Device counters written by the round kernels and read back between rounds.
+// One block per search side (forward / backward run in the same launches).
 struct Counters {
   unsigned long long next;       // items appended to the next frontier
   unsigned long long next_edges; // out-edges of the appended items (direction heuristic)
@@ -56,9 +57,13 @@ struct Counters {
   unsigned long long fail;       // failed table inserts (table needs to grow)
   unsigned long long edges;      // edges scanned (algorithmic bytes)
   unsigned long long probes;     // table slots probed (algorithmic bytes)
-  unsigned long long aux0;       // kernel-specific
-  unsigned long long aux1;
+  unsigned long long aux0;       // kernel-specific (queue cursor of bitmap -> queue)
+  unsigned long long aux1;       // kernel-specific (re-queued pairs)
+  unsigned long long expanded;   // vertices whose adjacency was read
+  unsigned long long unvisited;  // vertices examined by a pull round
+  unsigned long long pad[6];
 };
+constexpr int kCounterSets = 4;
 
 // ---------------------------------------------------------------------------
 // Host-side helpers
@@ -94,7 +99,7 @@ struct psc_graph_s {
   int num_sms = 0;
   // named scratch buffers, grown on demand (stream-ordered allocator)
   std::vector<psc::DevBuf> bufs;
-  psc::Counters* ctr = nullptr;   // device
+  psc::Counters* ctr = nullptr;   // device, kCounterSets blocks
   psc::Counters* hctr = nullptr;  // pinned host mirror
   // statistics / profiling
   psc_stats_t stats{};
@@ -131,6 +136,11 @@ enum Buf : int {
   B_PA,           // u64 pair frontier A
   B_PB,           // u64 pair frontier B
   B_PH,           // u64 pair heavy list
+  B_QA2,          // second search side (backward) of a two-sided reach
+  B_QB2,
+  B_FB_A2,
+  B_FB_B2,
+  B_HEAVY2,
   B_AUX0,
   B_AUX1,
   B_AUX2,

@@ -17,6 +17,10 @@ int build_transpose(psc_graph_s* g);
 int reach_run(psc_graph_s* g, uint32_t src, bool backward, bool local, uint32_t tau,
               uint32_t pull_div, uint32_t* vis, uint32_t* rounds);
 
+// Forward and backward reachability from one source, run together.
+int reach_pair(psc_graph_s* g, uint32_t src, bool local, uint32_t tau, uint32_t pull_div,
+               uint32_t* vis_f, uint32_t* vis_b, uint32_t* rounds_f, uint32_t* rounds_b);
+
 // SCC into device labels (u64[n]).
 int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* d_labels);
 

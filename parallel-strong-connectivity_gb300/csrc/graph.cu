@@ -66,12 +66,13 @@ int ensure_keep(psc_graph_s* g, int b, size_t bytes, size_t keep, void** out) {
 void swap_bufs(psc_graph_s* g, int a, int b) { std::swap(g->bufs[a], g->bufs[b]); }
 
 int zero_counters(psc_graph_s* g) {
-  PSC_CUDA(cudaMemsetAsync(g->ctr, 0, sizeof(Counters), g->stream));
+  PSC_CUDA(cudaMemsetAsync(g->ctr, 0, kCounterSets * sizeof(Counters), g->stream));
   return PSC_OK;
 }
 
 int read_counters(psc_graph_s* g) {
-  PSC_CUDA(cudaMemcpyAsync(g->hctr, g->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, g->stream));
+  PSC_CUDA(cudaMemcpyAsync(g->hctr, g->ctr, kCounterSets * sizeof(Counters),
+                           cudaMemcpyDeviceToHost, g->stream));
   PSC_CUDA(cudaStreamSynchronize(g->stream));
   return PSC_OK;
 }
@@ -162,8 +163,8 @@ static int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
   cudaError_t e;
   if ((e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaMalloc(&g->ctr, sizeof(Counters))) != cudaSuccess ||
-      (e = cudaMallocHost(&g->hctr, sizeof(Counters))) != cudaSuccess ||
+      (e = cudaMalloc(&g->ctr, kCounterSets * sizeof(Counters))) != cudaSuccess ||
+      (e = cudaMallocHost(&g->hctr, kCounterSets * sizeof(Counters))) != cudaSuccess ||
       (e = cudaEventCreate(&g->t0)) != cudaSuccess || (e = cudaEventCreate(&g->t1)) != cudaSuccess ||
       (e = cudaEventCreate(&g->u0)) != cudaSuccess || (e = cudaEventCreate(&g->u1)) != cudaSuccess ||
       (e = cudaEventCreate(&g->ph[0])) != cudaSuccess || (e = cudaEventCreate(&g->ph[1])) != cudaSuccess ||

@@ -1,23 +1,28 @@
 // Single-source reachability on the device (REACH, src/reach.hpp:21-243).
 //
-// Frontier rounds switch between
+// A search "side" is one direction from one source.  The first pivot of SCC
+// needs a forward and a backward side; both run in the same launches, so the
+// two latency-bound searches overlap.  Each round, per side:
 //   push: the frontier is a u32 queue; warps expand 32 frontier vertices at a
-//         time with the balanced warp expansion, claim targets with an
-//         atomicOr on the visited bitmap and append winners with one
-//         warp-aggregated atomic (the reference's hashbag insert + pack);
-//         vertices above kHeavyDeg out-edges go to a heavy list that the
-//         whole grid expands next;
+//         time with the balanced warp expansion, claim targets on the visited
+//         bitmap and append winners with one warp-aggregated atomic (the
+//         reference's hashbag insert + pack); vertices above kHeavyDeg
+//         out-edges go to a heavy list that the whole grid expands next;
+//   VGC:  (local search, reach.hpp:114-171) one frontier vertex per warp runs
+//         a local BFS in a shared-memory queue of up to tau vertices before
+//         spilling the rest to the next frontier — used while the frontier is
+//         small, where rounds, not bandwidth, bound the search;
 //   pull: the frontier is a bitmap; each warp owns 32 consecutive unvisited
 //         vertices and scans their in-edges until a frontier bit is found,
 //         then writes the visited / next-frontier words with one store
-//         (the reference's dense_update, no atomics needed).
-// The switch follows the reference's rule (judge, reach.hpp:86-112): push
-// while frontier vertices + their out-edges < m / pull_div (pull_div = 20),
-// with exact degree sums gathered by the kernels instead of sampling.
+//         (the reference's dense_update, no atomics).
+// The push/pull switch follows the reference's rule (judge, reach.hpp:86-112):
+// push while frontier vertices + their out-edges < m / pull_div (20), with
+// exact degree sums gathered by the kernels instead of sampling.
 //
-// VGC (local search, reach.hpp:114-171) runs each low-degree frontier vertex
-// as a warp-local BFS in shared memory that claims up to tau vertices in the
-// same round before spilling the rest to the global frontier.
+// Expansion issues K edges per lane before using any of them, so the loads of
+// E and the claims on the bitmap overlap instead of forming one dependent
+// memory round trip per edge.
 #include <mutex>
 
 #include "common.cuh"
@@ -27,72 +32,161 @@ namespace psc {
 
 constexpr int kReachBlock = 256;
 constexpr int kVgcQueue = 512;  // VGC queue entries per warp (16 KB per block)
+constexpr int kExpandK = 4;     // edges in flight per lane
+
+// One search side as the kernels see it.
+struct ReachSide {
+  const uint64_t* off;  // adjacency of the search direction
+  const uint32_t* E;
+  const uint32_t* qin;  // current frontier (queue)
+  uint64_t nin;
+  uint32_t* vis;        // visited bitmap
+  uint32_t* qout;       // next frontier (queue)
+  uint32_t* heavy;      // heavy list
+  Counters* ctr;
+};
 
 __global__ void k_reach_init(uint32_t* vis, uint32_t* q, uint32_t src) {
   vis[src >> 5] = 1u << (src & 31);
   q[0] = src;
 }
 
+__device__ __forceinline__ int find_src(const WarpExpandSmem& sm, uint32_t gi) {
+  int lo = 0, hi = 31;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (sm.excl[mid] <= gi)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Balanced expansion of the 32 lanes' ranges [beg, beg+deg) with K edges per
+// lane in flight.  CHECK = read the bitmap word before the atomic (fewer
+// atomics when most targets are visited; one more round trip otherwise).
+// emit(take, v) is called by every lane (warp-collective).
+template <int K, bool CHECK, class Emit>
+__device__ __forceinline__ void expand_claim(WarpExpandSmem& sm, uint64_t beg, uint32_t deg,
+                                             const uint32_t* __restrict__ E, uint32_t* vis,
+                                             Emit&& emit) {
+  const unsigned lane = lane_id();
+  uint32_t incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(kFull, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  sm.excl[lane] = incl - deg;
+  sm.beg[lane] = beg;
+  __syncwarp();
+  for (uint32_t base = 0; base < total; base += 32 * K) {
+    uint32_t v[K];
+    bool take[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t gi = base + k * 32 + lane;
+      v[k] = 0xFFFFFFFFu;
+      if (gi < total) {
+        const int s = find_src(sm, gi);
+        v[k] = __ldg(&E[sm.beg[s] + (gi - sm.excl[s])]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      take[k] = false;
+      if (v[k] != 0xFFFFFFFFu) {
+        const uint32_t b = 1u << (v[k] & 31);
+        if (!CHECK || !(__ldcg(&vis[v[k] >> 5]) & b)) take[k] = true;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (take[k]) {
+        const uint32_t b = 1u << (v[k] & 31);
+        take[k] = !(atomicOr(&vis[v[k] >> 5], b) & b);
+      }
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (base + k * 32 < total) emit(take[k], v[k]);
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void flush_side_counters(Counters* c0, Counters* c1,
+                                                    unsigned long long s0, unsigned long long s1,
+                                                    unsigned long long n0, unsigned long long n1,
+                                                    unsigned long long x0, unsigned long long x1) {
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  n0 = warp_sum(n0);
+  n1 = warp_sum(n1);
+  x0 = warp_sum(x0);
+  x1 = warp_sum(x1);
+  if (lane_id() == 0) {
+    if (s0 | n0 | x0) {
+      atomicAdd(&c0->edges, s0);
+      atomicAdd(&c0->next_edges, n0);
+      atomicAdd(&c0->expanded, x0);
+    }
+    if (s1 | n1 | x1) {
+      atomicAdd(&c1->edges, s1);
+      atomicAdd(&c1->next_edges, n1);
+      atomicAdd(&c1->expanded, x1);
+    }
+  }
+}
+
+// Push round for up to two sides: 32 frontier vertices per warp step.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
-    k_reach_push(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
-                 const uint32_t* __restrict__ qin, uint64_t nin, uint32_t* vis, uint32_t* qout,
-                 uint32_t* heavy, Counters* ctr) {
+__global__ void __launch_bounds__(BLOCK) k_reach_push(ReachSide s0, ReachSide s1) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
-  unsigned long long scanned = 0, next_edges = 0;
-  for (uint64_t base = gw * 32; base < nin; base += nw * 32) {
-    const uint64_t i = base + lane;
+  const uint64_t c0 = (s0.nin + 31) / 32, c1 = (s1.nin + 31) / 32;
+  unsigned long long scanned0 = 0, scanned1 = 0, nedges0 = 0, nedges1 = 0, exp0 = 0, exp1 = 0;
+  for (uint64_t c = gw; c < c0 + c1; c += nw) {
+    const int sd = c < c0 ? 0 : 1;
+    const ReachSide S = sd ? s1 : s0;
+    const uint64_t i = (sd ? c - c0 : c) * 32 + lane;
     uint64_t beg = 0;
     uint32_t deg = 0;
-    if (i < nin) {
-      uint32_t u = qin[i];
-      beg = off[u];
-      uint64_t d = off[u + 1] - beg;
+    if (i < S.nin) {
+      const uint32_t u = S.qin[i];
+      beg = S.off[u];
+      uint64_t d = S.off[u + 1] - beg;
+      (sd ? exp1 : exp0)++;
       if (d > kHeavyDeg) {
-        heavy[atomicAdd(&ctr->heavy, 1ull)] = u;
+        S.heavy[atomicAdd(&S.ctr->heavy, 1ull)] = u;
         d = 0;
       }
       deg = (uint32_t)d;
     }
-    scanned += deg;
-    warp_expand(sm[wid], beg, deg, [&](bool act, int, uint64_t e) {
-      uint32_t v = 0;
-      bool take = false;
-      if (act) {
-        v = __ldg(&E[e]);
-        take = bit_set(vis, v);
-      }
-      unsigned long long pos = warp_append(&ctr->next, take);
+    (sd ? scanned1 : scanned0) += deg;
+    expand_claim<kExpandK, true>(sm[wid], beg, deg, S.E, S.vis, [&](bool take, uint32_t v) {
+      unsigned long long pos = warp_append(&S.ctr->next, take);
       if (take) {
-        qout[pos] = v;
-        next_edges += off[v + 1] - off[v];
+        S.qout[pos] = v;
+        (sd ? nedges1 : nedges0) += S.off[v + 1] - S.off[v];
       }
     });
   }
-  scanned = warp_sum(scanned);
-  next_edges = warp_sum(next_edges);
-  if (lane == 0) {
-    if (scanned) atomicAdd(&ctr->edges, scanned);
-    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
-  }
+  flush_side_counters(s0.ctr, s1.ctr, scanned0, scanned1, nedges0, nedges1, exp0, exp1);
 }
 
-// VGC push round (reach.hpp:114-171): one frontier vertex per warp.  A vertex
-// with 0 < deg < tau starts a local BFS in a shared-memory queue of tq =
-// min(tau, QCAP) entries: the warp expands up to 32 queued vertices per wave
-// with the balanced expansion, claims neighbours on the visited bitmap, and
-// keeps a claimed vertex in the queue while it has room, else spills it to the
-// next global frontier.  Queued vertices with more than tq out-edges, and
-// whatever is left in the queue when it fills, are spilled as well.  Other
-// frontier vertices are expanded directly (heavy ones by the whole grid).
+// VGC round for up to two sides: one frontier vertex per warp.  A vertex with
+// 0 < deg < tau starts a local BFS in a shared-memory queue of tq =
+// min(tau, QCAP) entries: the warp expands up to 32 queued vertices per wave,
+// claims neighbours on the bitmap, and keeps a claimed vertex in the queue
+// while it has room, else spills it to the next frontier.  Queued vertices
+// with more than tq out-edges, and whatever is left in the queue when it
+// fills, are spilled too.  Other frontier vertices are expanded directly
+// (heavy ones by the whole grid).
 template <int BLOCK, int QCAP>
-__global__ void __launch_bounds__(BLOCK)
-    k_reach_vgc(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
-                const uint32_t* __restrict__ qin, uint64_t nin, uint32_t* vis, uint32_t* qout,
-                uint32_t* heavy, Counters* ctr, uint32_t tau) {
+__global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ uint32_t sq[BLOCK / 32][QCAP];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -100,31 +194,34 @@ __global__ void __launch_bounds__(BLOCK)
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
   uint32_t* Q = sq[wid];
-  unsigned long long scanned = 0, next_edges = 0;
-  auto emit = [&](bool take, uint32_t v) {
-    unsigned long long pos = warp_append(&ctr->next, take);
-    if (take) {
-      qout[pos] = v;
-      next_edges += off[v + 1] - off[v];
-    }
-  };
-  for (uint64_t i = gw; i < nin; i += nw) {
-    const uint32_t u = qin[i];
-    const uint64_t ub = off[u], ue = off[u + 1];
+  unsigned long long scanned0 = 0, scanned1 = 0, nedges0 = 0, nedges1 = 0, exp0 = 0, exp1 = 0;
+  for (uint64_t i = gw; i < s0.nin + s1.nin; i += nw) {
+    const int sd = i < s0.nin ? 0 : 1;
+    const ReachSide S = sd ? s1 : s0;
+    auto emit = [&](bool take, uint32_t v) {
+      unsigned long long pos = warp_append(&S.ctr->next, take);
+      if (take) {
+        S.qout[pos] = v;
+        (sd ? nedges1 : nedges0) += S.off[v + 1] - S.off[v];
+      }
+    };
+    const uint32_t u = S.qin[sd ? i - s0.nin : i];
+    const uint64_t ub = S.off[u], ue = S.off[u + 1];
     const uint64_t du = ue - ub;
+    if (lane == 0) (sd ? exp1 : exp0)++;
     if (!(du > 0 && du < tq)) {
       if (du > kHeavyDeg) {
-        if (lane == 0) heavy[atomicAdd(&ctr->heavy, 1ull)] = u;
+        if (lane == 0) S.heavy[atomicAdd(&S.ctr->heavy, 1ull)] = u;
         continue;
       }
-      if (lane == 0) scanned += du;
+      if (lane == 0) (sd ? scanned1 : scanned0) += du;
       for (uint64_t b = ub; b < ue; b += 32) {
         const uint64_t e = b + lane;
         uint32_t v = 0;
         bool take = false;
         if (e < ue) {
-          v = __ldg(&E[e]);
-          take = bit_set(vis, v);
+          v = __ldg(&S.E[e]);
+          take = bit_set(S.vis, v);
         }
         emit(take, v);
       }
@@ -140,25 +237,20 @@ __global__ void __launch_bounds__(BLOCK)
       bool spill_self = false;
       if (lane < wave) {
         x = Q[head + lane];
-        beg = off[x];
-        uint64_t d = off[x + 1] - beg;
+        beg = S.off[x];
+        uint64_t d = S.off[x + 1] - beg;
         if (d > tq) {
           spill_self = true;
           d = 0;
         }
         deg = (uint32_t)d;
+        if (lane > 0 || head > 0) (sd ? exp1 : exp0)++;
       }
       head += wave;
       __syncwarp();
       emit(spill_self, x);
-      scanned += deg;
-      warp_expand(sm[wid], beg, deg, [&](bool act, int, uint64_t e) {
-        uint32_t v = 0;
-        bool take = false;
-        if (act) {
-          v = __ldg(&E[e]);
-          take = bit_set(vis, v);
-        }
+      (sd ? scanned1 : scanned0) += deg;
+      expand_claim<kExpandK, false>(sm[wid], beg, deg, S.E, S.vis, [&](bool take, uint32_t v) {
         const unsigned mask = __ballot_sync(kFull, take);
         const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
         const uint32_t room = tq - tail;
@@ -168,7 +260,6 @@ __global__ void __launch_bounds__(BLOCK)
         tail += nt < room ? nt : room;
         emit(take && !local, v);
       });
-      __syncwarp();
     }
     for (uint32_t b = head; b < tail; b += 32) {
       const uint32_t k = b + lane;
@@ -177,53 +268,51 @@ __global__ void __launch_bounds__(BLOCK)
     }
     __syncwarp();
   }
-  scanned = warp_sum(scanned);
-  next_edges = warp_sum(next_edges);
-  if (lane == 0) {
-    if (scanned) atomicAdd(&ctr->edges, scanned);
-    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
-  }
+  flush_side_counters(s0.ctr, s1.ctr, scanned0, scanned1, nedges0, nedges1, exp0, exp1);
 }
 
-// The whole grid walks the edges of every heavy vertex, 32 edges per warp step.
+// The whole grid walks the edges of every heavy vertex of both sides, 32
+// edges per warp step.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
-    k_reach_heavy(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
-                  const uint32_t* __restrict__ heavy, Counters* ctr, uint32_t* vis, uint32_t* qout) {
+__global__ void __launch_bounds__(BLOCK) k_reach_heavy(ReachSide s0, ReachSide s1) {
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const uint64_t nh = *(volatile unsigned long long*)&ctr->heavy;
   const uint64_t stride = (uint64_t)gridDim.x * BLOCK;
-  unsigned long long scanned = 0, next_edges = 0;
-  for (uint64_t h = 0; h < nh; h++) {
-    const uint32_t u = heavy[h];
-    const uint64_t beg = off[u], end = off[u + 1];
-    for (uint64_t b = beg + (uint64_t)blockIdx.x * BLOCK + wid * 32; b < end; b += stride) {
-      const uint64_t e = b + lane;
-      const bool act = e < end;
-      uint32_t v = 0;
-      bool take = false;
-      if (act) {
-        scanned++;
-        v = __ldg(&E[e]);
-        take = bit_set(vis, v);
-      }
-      unsigned long long pos = warp_append(&ctr->next, take);
-      if (take) {
-        qout[pos] = v;
-        next_edges += off[v + 1] - off[v];
+#pragma unroll 1
+  for (int sd = 0; sd < 2; sd++) {
+    const ReachSide S = sd ? s1 : s0;
+    if (!S.ctr) continue;
+    const uint64_t nh = *(volatile unsigned long long*)&S.ctr->heavy;
+    unsigned long long scanned = 0, next_edges = 0;
+    for (uint64_t h = 0; h < nh; h++) {
+      const uint32_t u = S.heavy[h];
+      const uint64_t beg = S.off[u], end = S.off[u + 1];
+      for (uint64_t b = beg + (uint64_t)blockIdx.x * BLOCK + wid * 32; b < end; b += stride) {
+        const uint64_t e = b + lane;
+        uint32_t v = 0;
+        bool take = false;
+        if (e < end) {
+          scanned++;
+          v = __ldg(&S.E[e]);
+          take = bit_set(S.vis, v);
+        }
+        unsigned long long pos = warp_append(&S.ctr->next, take);
+        if (take) {
+          S.qout[pos] = v;
+          next_edges += S.off[v + 1] - S.off[v];
+        }
       }
     }
-  }
-  scanned = warp_sum(scanned);
-  next_edges = warp_sum(next_edges);
-  if (lane == 0) {
-    if (scanned) atomicAdd(&ctr->edges, scanned);
-    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
+    scanned = warp_sum(scanned);
+    next_edges = warp_sum(next_edges);
+    if (lane == 0) {
+      if (scanned) atomicAdd(&S.ctr->edges, scanned);
+      if (next_edges) atomicAdd(&S.ctr->next_edges, next_edges);
+    }
   }
 }
 
-// Pull round: B_* is the reverse direction of the search, A_off the forward
-// offsets (for the next round's edge count).
+// Pull round: B_* is the reverse direction of the search, A_off the search
+// direction's offsets (for the next round's edge count).
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
@@ -233,12 +322,13 @@ __global__ void __launch_bounds__(BLOCK)
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint64_t nwords = (n + 31) >> 5;
-  unsigned long long cnt = 0, scanned = 0, next_edges = 0;
+  unsigned long long cnt = 0, scanned = 0, next_edges = 0, unvisited = 0;
   for (uint64_t w = gw; w < nwords; w += nw) {
     const uint64_t v = w * 32 + lane;
     const uint32_t vw = vis[w];
     bool found = false;
     if (v < n && !((vw >> lane) & 1u)) {
+      unvisited++;
       const uint64_t b = B_off[v], e = B_off[v + 1];
       uint64_t j = b;
       for (; j < e; j++) {
@@ -260,10 +350,12 @@ __global__ void __launch_bounds__(BLOCK)
   }
   scanned = warp_sum(scanned);
   next_edges = warp_sum(next_edges);
+  unvisited = warp_sum(unvisited);
   if (lane == 0) {
     if (cnt) atomicAdd(&ctr->next, cnt);
     if (scanned) atomicAdd(&ctr->edges, scanned);
     if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
+    if (unvisited) atomicAdd(&ctr->unvisited, unvisited);
   }
 }
 
@@ -303,82 +395,187 @@ __global__ void k_bitmap_to_queue(const uint32_t* __restrict__ fb, uint64_t nwor
   }
 }
 
-int reach_run(psc_graph_s* g, uint32_t src, bool backward, bool local, uint32_t tau,
-              uint32_t pull_div, uint32_t* vis, uint32_t* rounds_out) {
-  const uint64_t n = g->n, nwords = (n + 31) / 32;
-  // VGC rounds while the frontier is below one vertex per resident warp
-  const uint64_t vgc_limit = (uint64_t)g->num_sms * 64;
-  const uint64_t* A_off = backward ? g->in_off : g->off;
-  const uint32_t* A_E = backward ? g->in_E : g->E;
-  const uint64_t* B_off = backward ? g->off : g->in_off;
-  const uint32_t* B_E = backward ? g->E : g->in_E;
-  uint32_t *qa, *qb, *fa, *fb, *heavy;
-  PSC_TRY(ensure_t(g, B_QA, n + 1, &qa));
-  PSC_TRY(ensure_t(g, B_QB, n + 1, &qb));
-  PSC_TRY(ensure_t(g, B_FB_A, nwords + 1, &fa));
-  PSC_TRY(ensure_t(g, B_FB_B, nwords + 1, &fb));
-  PSC_TRY(ensure_t(g, B_HEAVY, n + 1, &heavy));
-  PSC_CUDA(cudaMemsetAsync(vis, 0, nwords * 4, g->stream));
-  k_reach_init<<<1, 1, 0, g->stream>>>(vis, qa, src);
-  if (pull_div == 0) pull_div = 20;
-  const uint64_t threshold = g->m / pull_div;
-  uint64_t nf = 1, nf_edges = 0;
-  bool pull = false;
-  uint32_t rounds = 0;
-  while (nf > 0) {
-    rounds++;
-    if (rounds > n + 2) return PSC_ERR_ITER_LIMIT;
-    const bool want_pull = (nf + nf_edges) >= threshold;
-    if (want_pull && !pull) {
-      ProfScope ps(g, F_REACH_PULL);
-      PSC_CUDA(cudaMemsetAsync(fa, 0, nwords * 4, g->stream));
-      k_queue_to_bitmap<<<grid_for(g, nf, 256), 256, 0, g->stream>>>(qa, nf, fa);
-      pull = true;
-    } else if (!want_pull && pull) {
-      ProfScope ps(g, F_REACH_PUSH);
-      PSC_TRY(zero_counters(g));
-      k_bitmap_to_queue<<<grid_for(g, nwords, 256), 256, 0, g->stream>>>(fa, nwords, qa, g->ctr);
-      pull = false;
-    }
-    PSC_TRY(zero_counters(g));
-    if (!pull) {
-      if (local && nf <= vgc_limit) {
-        ProfScope ps(g, F_REACH_VGC);
-        k_reach_vgc<kReachBlock, kVgcQueue>
-            <<<grid_for(g, nf * 32, kReachBlock), kReachBlock, 0, g->stream>>>(
-                A_off, A_E, qa, nf, vis, qb, heavy, g->ctr, tau ? tau : 512);
-      } else {
-        ProfScope ps(g, F_REACH_PUSH);
-        k_reach_push<kReachBlock><<<grid_for(g, nf, kReachBlock), kReachBlock, 0, g->stream>>>(
-            A_off, A_E, qa, nf, vis, qb, heavy, g->ctr);
-      }
-      {
-        ProfScope ps(g, F_HEAVY);
-        k_reach_heavy<kReachBlock><<<g->num_sms * 4, kReachBlock, 0, g->stream>>>(A_off, A_E, heavy,
-                                                                                  g->ctr, vis, qb);
-      }
-      std::swap(qa, qb);
-      swap_bufs(g, B_QA, B_QB);
-    } else {
-      ProfScope ps(g, F_REACH_PULL);
-      k_reach_pull<kReachBlock><<<grid_for(g, nwords * 32, kReachBlock), kReachBlock, 0, g->stream>>>(
-          B_off, B_E, A_off, fa, vis, fb, n, g->ctr);
-      std::swap(fa, fb);
-      swap_bufs(g, B_FB_A, B_FB_B);
-    }
-    PSC_CUDA(cudaGetLastError());
-    PSC_TRY(read_counters(g));
-    nf = g->hctr->next;
-    nf_edges = g->hctr->next_edges;
-  }
-  if (rounds_out) *rounds_out = rounds;
-  return PSC_OK;
-}
-
 __global__ void k_bitmap_to_bytes(const uint32_t* __restrict__ vis, uint64_t n, uint8_t* out) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x)
     out[i] = (vis[i >> 5] >> (i & 31)) & 1u;
+}
+
+// ---------------------------------------------------------------------------
+// Host round loop over one or two sides.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Side {
+  bool backward = false;
+  uint32_t* vis = nullptr;
+  int slot_qa = 0, slot_qb = 0, slot_fa = 0, slot_fb = 0, slot_heavy = 0;
+  int cset = 0;  // counter block
+  uint64_t nf = 0, nf_edges = 0;
+  bool pull = false;
+  uint32_t rounds = 0;
+};
+
+enum Mode { M_NONE, M_VGC, M_PUSH, M_PULL };
+
+ReachSide side_args(psc_graph_s* g, const Side& s) {
+  ReachSide r;
+  r.off = s.backward ? g->in_off : g->off;
+  r.E = s.backward ? g->in_E : g->E;
+  r.qin = (const uint32_t*)g->bufs[s.slot_qa].p;
+  r.nin = s.nf;
+  r.vis = s.vis;
+  r.qout = (uint32_t*)g->bufs[s.slot_qb].p;
+  r.heavy = (uint32_t*)g->bufs[s.slot_heavy].p;
+  r.ctr = g->ctr + s.cset;
+  return r;
+}
+
+Side make_side(bool backward, uint32_t* vis, int second) {
+  Side s;
+  s.backward = backward;
+  s.vis = vis;
+  s.slot_qa = second ? B_QA2 : B_QA;
+  s.slot_qb = second ? B_QB2 : B_QB;
+  s.slot_fa = second ? B_FB_A2 : B_FB_A;
+  s.slot_fb = second ? B_FB_B2 : B_FB_B;
+  s.slot_heavy = second ? B_HEAVY2 : B_HEAVY;
+  s.cset = second ? 1 : 0;
+  return s;
+}
+
+}  // namespace
+
+// Runs the searches of `ns` sides (1 or 2) to completion.
+static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs, bool local,
+                       uint32_t tau, uint32_t pull_div) {
+  const uint64_t n = g->n, nwords = (n + 31) / 32;
+  // VGC rounds while the frontier is below one vertex per resident warp
+  const uint64_t vgc_limit = (uint64_t)g->num_sms * 64;
+  if (pull_div == 0) pull_div = 20;
+  const uint64_t threshold = g->m / pull_div;
+  for (int k = 0; k < ns; k++) {
+    Side& s = sides[k];
+    void* p;
+    PSC_TRY(ensure(g, s.slot_qa, (n + 1) * 4, &p));
+    PSC_TRY(ensure(g, s.slot_qb, (n + 1) * 4, &p));
+    PSC_TRY(ensure(g, s.slot_fa, (nwords + 1) * 4, &p));
+    PSC_TRY(ensure(g, s.slot_fb, (nwords + 1) * 4, &p));
+    PSC_TRY(ensure(g, s.slot_heavy, (n + 1) * 4, &p));
+    PSC_CUDA(cudaMemsetAsync(s.vis, 0, nwords * 4, g->stream));
+    k_reach_init<<<1, 1, 0, g->stream>>>(s.vis, (uint32_t*)g->bufs[s.slot_qa].p, srcs[k]);
+    s.nf = 1;
+    s.nf_edges = 0;
+    s.pull = false;
+    s.rounds = 0;
+  }
+  for (uint64_t iter = 0;; iter++) {
+    if (iter > n + 2) return PSC_ERR_ITER_LIMIT;
+    Mode mode[2] = {M_NONE, M_NONE};
+    bool any = false;
+    for (int k = 0; k < ns; k++) {
+      Side& s = sides[k];
+      if (s.nf == 0) continue;
+      any = true;
+      s.rounds++;
+      const bool want_pull = (s.nf + s.nf_edges) >= threshold;
+      uint32_t* qa = (uint32_t*)g->bufs[s.slot_qa].p;
+      uint32_t* fa = (uint32_t*)g->bufs[s.slot_fa].p;
+      if (want_pull && !s.pull) {
+        ProfScope ps(g, F_REACH_PULL);
+        PSC_CUDA(cudaMemsetAsync(fa, 0, nwords * 4, g->stream));
+        k_queue_to_bitmap<<<grid_for(g, s.nf, 256), 256, 0, g->stream>>>(qa, s.nf, fa);
+        s.pull = true;
+      } else if (!want_pull && s.pull) {
+        ProfScope ps(g, F_REACH_PUSH);
+        PSC_CUDA(cudaMemsetAsync(&g->ctr[s.cset].aux0, 0, 8, g->stream));
+        k_bitmap_to_queue<<<grid_for(g, nwords, 256), 256, 0, g->stream>>>(fa, nwords, qa,
+                                                                         g->ctr + s.cset);
+        s.pull = false;
+      }
+      mode[k] = s.pull ? M_PULL : (local && s.nf <= vgc_limit) ? M_VGC : M_PUSH;
+    }
+    if (!any) break;
+    PSC_TRY(zero_counters(g));
+    ReachSide vg[2] = {}, pu[2] = {}, hv[2] = {};
+    int nv = 0, np = 0, nh = 0;
+    uint64_t v_items = 0, p_items = 0;
+    for (int k = 0; k < ns; k++) {
+      if (mode[k] == M_VGC) {
+        vg[nv++] = side_args(g, sides[k]);
+        v_items += sides[k].nf;
+      } else if (mode[k] == M_PUSH) {
+        pu[np++] = side_args(g, sides[k]);
+        p_items += sides[k].nf;
+      }
+      if (mode[k] == M_VGC || mode[k] == M_PUSH) hv[nh++] = side_args(g, sides[k]);
+    }
+    if (nv) {
+      ProfScope ps(g, F_REACH_VGC);
+      k_reach_vgc<kReachBlock, kVgcQueue>
+          <<<grid_for(g, v_items * 32, kReachBlock), kReachBlock, 0, g->stream>>>(vg[0], vg[1], tau);
+    }
+    if (np) {
+      ProfScope ps(g, F_REACH_PUSH);
+      k_reach_push<kReachBlock><<<grid_for(g, p_items, kReachBlock), kReachBlock, 0, g->stream>>>(
+          pu[0], pu[1]);
+    }
+    if (nh) {
+      ProfScope ps(g, F_HEAVY);
+      k_reach_heavy<kReachBlock><<<g->num_sms * 4, kReachBlock, 0, g->stream>>>(hv[0], hv[1]);
+    }
+    for (int k = 0; k < ns; k++) {
+      if (mode[k] != M_PULL) continue;
+      Side& s = sides[k];
+      ProfScope ps(g, F_REACH_PULL);
+      k_reach_pull<kReachBlock><<<grid_for(g, nwords * 32, kReachBlock), kReachBlock, 0, g->stream>>>(
+          s.backward ? g->off : g->in_off, s.backward ? g->E : g->in_E,
+          s.backward ? g->in_off : g->off, (const uint32_t*)g->bufs[s.slot_fa].p, s.vis,
+          (uint32_t*)g->bufs[s.slot_fb].p, n, g->ctr + s.cset);
+    }
+    PSC_CUDA(cudaGetLastError());
+    PSC_TRY(read_counters(g));
+    for (int k = 0; k < ns; k++) {
+      Side& s = sides[k];
+      if (mode[k] == M_NONE) continue;
+      const Counters& c = g->hctr[s.cset];
+      if (g->profiling) {
+        // algorithmic bytes: 16 per adjacency range read, 4 + 1 per edge
+        // (target id, visited flag), 5 per new frontier vertex; pull: 16 per
+        // unvisited vertex, 5 per scanned in-edge, bitmap words 1/4 byte per vertex
+        const int fam = mode[k] == M_VGC ? F_REACH_VGC : mode[k] == M_PUSH ? F_REACH_PUSH
+                                                                           : F_REACH_PULL;
+        g->prof[fam].bytes += mode[k] == M_PULL
+                                  ? 16.0 * c.unvisited + 5.0 * c.edges + 0.25 * n + 1.0 * c.next
+                                  : 16.0 * c.expanded + 5.0 * c.edges + 5.0 * c.next;
+      }
+      if (mode[k] == M_PULL)
+        std::swap(g->bufs[s.slot_fa], g->bufs[s.slot_fb]);
+      else
+        std::swap(g->bufs[s.slot_qa], g->bufs[s.slot_qb]);
+      s.nf = c.next;
+      s.nf_edges = c.next_edges;
+    }
+  }
+  return PSC_OK;
+}
+
+int reach_run(psc_graph_s* g, uint32_t src, bool backward, bool local, uint32_t tau,
+              uint32_t pull_div, uint32_t* vis, uint32_t* rounds_out) {
+  Side s = make_side(backward, vis, 0);
+  PSC_TRY(reach_sides(g, &s, 1, &src, local, tau ? tau : 512, pull_div));
+  if (rounds_out) *rounds_out = s.rounds;
+  return PSC_OK;
+}
+
+int reach_pair(psc_graph_s* g, uint32_t src, bool local, uint32_t tau, uint32_t pull_div,
+               uint32_t* vis_f, uint32_t* vis_b, uint32_t* rounds_f, uint32_t* rounds_b) {
+  Side s[2] = {make_side(false, vis_f, 0), make_side(true, vis_b, 1)};
+  const uint32_t srcs[2] = {src, src};
+  PSC_TRY(reach_sides(g, s, 2, srcs, local, tau ? tau : 512, pull_div));
+  if (rounds_f) *rounds_f = s[0].rounds;
+  if (rounds_b) *rounds_b = s[1].rounds;
+  return PSC_OK;
 }
 
 }  // namespace psc
@@ -520,10 +717,11 @@ extern "C" int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E,
     }
     PSC_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), s));
     if (!pull) {
-      k_reach_push<kReachBlock><<<na_grid(nd.num_sms, nf, kReachBlock), kReachBlock, 0, s>>>(
-          A_off, A_E, qa, nf, vis, qb, heavy, ctr);
-      k_reach_heavy<kReachBlock><<<nd.num_sms * 4, kReachBlock, 0, s>>>(A_off, A_E, heavy, ctr,
-                                                                       vis, qb);
+      ReachSide side{A_off, A_E, qa, nf, vis, qb, heavy, ctr};
+      ReachSide none{};
+      k_reach_push<kReachBlock><<<na_grid(nd.num_sms, nf, kReachBlock), kReachBlock, 0, s>>>(side,
+                                                                                          none);
+      k_reach_heavy<kReachBlock><<<nd.num_sms * 4, kReachBlock, 0, s>>>(side, none);
       std::swap(qa, qb);
     } else {
       k_reach_pull<kReachBlock><<<na_grid(nd.num_sms, nwords * 32, kReachBlock), kReachBlock, 0, s>>>(

@@ -589,8 +589,7 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
     PSC_TRY(ensure_t(g, B_VIS_F, (n + 31) / 32 + 1, &vf));
     PSC_TRY(ensure_t(g, B_VIS_B, (n + 31) / 32 + 1, &vb));
     uint32_t r1 = 0, r2 = 0;
-    PSC_TRY(reach_run(g, src, false, p->local_reach != 0, p->tau, p->pull_div, vf, &r1));
-    PSC_TRY(reach_run(g, src, true, p->local_reach != 0, p->tau, p->pull_div, vb, &r2));
+    PSC_TRY(reach_pair(g, src, p->local_reach != 0, p->tau, p->pull_div, vf, vb, &r1, &r2));
     g->stats.reach_rounds = r1 + r2;
     {
       ProfScope ps(g, F_LABEL_FIRST);

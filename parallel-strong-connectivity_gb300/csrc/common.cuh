@@ -141,6 +141,10 @@ enum Buf : int {
   B_FB_A2,
   B_FB_B2,
   B_HEAVY2,
+  B_PA2,          // second multi-search side's pair frontiers / heavy list / flags
+  B_PB2,
+  B_PH2,
+  B_HF2,
   B_AUX0,
   B_AUX1,
   B_AUX2,

@@ -31,8 +31,9 @@
 namespace psc {
 
 constexpr int kReachBlock = 256;
-constexpr int kVgcQueue = 512;  // VGC queue entries per warp (16 KB per block)
-constexpr int kExpandK = 4;     // edges in flight per lane
+constexpr int kVgcBlock = 128;  // VGC blocks: 4 warps
+constexpr int kVgcQueue = 512;  // VGC queue entries per warp (8 KB of 16-byte entries)
+constexpr int kExpandK = 8;     // edges in flight per lane
 
 // One search side as the kernels see it.
 struct ReachSide {
@@ -177,6 +178,70 @@ __global__ void __launch_bounds__(BLOCK) k_reach_push(ReachSide s0, ReachSide s1
   flush_side_counters(s0.ctr, s1.ctr, scanned0, scanned1, nedges0, nedges1, exp0, exp1);
 }
 
+// Like expand_claim without the pre-check, and each candidate's adjacency
+// range off[v], off[v+1] is loaded alongside its claim (speculatively: the
+// load is wasted when the claim fails), so a claimed vertex enters the local
+// queue with its range and the next wave needs no dependent offset load.
+// emit(take, v, vbeg, vdeg) is warp-collective.
+template <int K, class Emit>
+__device__ __forceinline__ void expand_claim_pf(WarpExpandSmem& sm, uint64_t beg, uint32_t deg,
+                                                const uint64_t* __restrict__ off,
+                                                const uint32_t* __restrict__ E, uint32_t* vis,
+                                                Emit&& emit) {
+  const unsigned lane = lane_id();
+  uint32_t incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(kFull, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  sm.excl[lane] = incl - deg;
+  sm.beg[lane] = beg;
+  __syncwarp();
+  for (uint32_t base = 0; base < total; base += 32 * K) {
+    uint32_t v[K];
+    uint64_t vb[K], ve[K];
+    bool take[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t gi = base + k * 32 + lane;
+      v[k] = 0xFFFFFFFFu;
+      if (gi < total) {
+        const int s = find_src(sm, gi);
+        v[k] = __ldg(&E[sm.beg[s] + (gi - sm.excl[s])]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      vb[k] = ve[k] = 0;
+      if (v[k] != 0xFFFFFFFFu) {
+        vb[k] = __ldg(&off[v[k]]);
+        ve[k] = __ldg(&off[v[k] + 1]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      take[k] = false;
+      if (v[k] != 0xFFFFFFFFu) {
+        const uint32_t b = 1u << (v[k] & 31);
+        take[k] = !(atomicOr(&vis[v[k] >> 5], b) & b);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (base + k * 32 < total) emit(take[k], v[k], vb[k], ve[k] - vb[k]);
+  }
+  __syncwarp();
+}
+
+// Local-queue entry: a claimed vertex with its adjacency range.
+struct QEnt {
+  uint64_t beg;
+  uint32_t v;
+  uint32_t deg;
+};
+
 // VGC round for up to two sides: one frontier vertex per warp.  A vertex with
 // 0 < deg < tau starts a local BFS in a shared-memory queue of tq =
 // min(tau, QCAP) entries: the warp expands up to 32 queued vertices per wave,
@@ -188,21 +253,21 @@ __global__ void __launch_bounds__(BLOCK) k_reach_push(ReachSide s0, ReachSide s1
 template <int BLOCK, int QCAP>
 __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
-  __shared__ uint32_t sq[BLOCK / 32][QCAP];
+  __shared__ QEnt sq[BLOCK / 32][QCAP];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
-  uint32_t* Q = sq[wid];
+  QEnt* Q = sq[wid];
   unsigned long long scanned0 = 0, scanned1 = 0, nedges0 = 0, nedges1 = 0, exp0 = 0, exp1 = 0;
   for (uint64_t i = gw; i < s0.nin + s1.nin; i += nw) {
     const int sd = i < s0.nin ? 0 : 1;
     const ReachSide S = sd ? s1 : s0;
-    auto emit = [&](bool take, uint32_t v) {
+    auto emit = [&](bool take, uint32_t v, uint64_t vdeg) {
       unsigned long long pos = warp_append(&S.ctr->next, take);
       if (take) {
         S.qout[pos] = v;
-        (sd ? nedges1 : nedges0) += S.off[v + 1] - S.off[v];
+        (sd ? nedges1 : nedges0) += vdeg;
       }
     };
     const uint32_t u = S.qin[sd ? i - s0.nin : i];
@@ -223,48 +288,52 @@ __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1,
           v = __ldg(&S.E[e]);
           take = bit_set(S.vis, v);
         }
-        emit(take, v);
+        emit(take, v, take ? S.off[v + 1] - S.off[v] : 0);
       }
       continue;
     }
-    if (lane == 0) Q[0] = u;
+    if (lane == 0) Q[0] = QEnt{ub, u, (uint32_t)du};
     __syncwarp();
     uint32_t head = 0, tail = 1;
     while (head < tail && tail < tq) {
       const uint32_t wave = min(32u, tail - head);
       uint64_t beg = 0;
-      uint32_t deg = 0, x = 0;
+      uint32_t deg = 0, x = 0, xdeg = 0;
       bool spill_self = false;
       if (lane < wave) {
-        x = Q[head + lane];
-        beg = S.off[x];
-        uint64_t d = S.off[x + 1] - beg;
-        if (d > tq) {
+        const QEnt q = Q[head + lane];
+        x = q.v;
+        beg = q.beg;
+        xdeg = q.deg;
+        deg = q.deg;
+        if (deg > tq) {
           spill_self = true;
-          d = 0;
+          deg = 0;
         }
-        deg = (uint32_t)d;
         if (lane > 0 || head > 0) (sd ? exp1 : exp0)++;
       }
       head += wave;
       __syncwarp();
-      emit(spill_self, x);
+      emit(spill_self, x, xdeg);
       (sd ? scanned1 : scanned0) += deg;
-      expand_claim<kExpandK, false>(sm[wid], beg, deg, S.E, S.vis, [&](bool take, uint32_t v) {
-        const unsigned mask = __ballot_sync(kFull, take);
-        const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
-        const uint32_t room = tq - tail;
-        const bool local = take && rank < room;
-        if (local) Q[tail + rank] = v;
-        const uint32_t nt = __popc(mask);
-        tail += nt < room ? nt : room;
-        emit(take && !local, v);
-      });
+      expand_claim_pf<kExpandK>(
+          sm[wid], beg, deg, S.off, S.E, S.vis, [&](bool take, uint32_t v, uint64_t vb, uint64_t vd) {
+            const unsigned mask = __ballot_sync(kFull, take);
+            const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
+            const uint32_t room = tq - tail;
+            const bool local = take && rank < room;
+            if (local) Q[tail + rank] = QEnt{vb, v, (uint32_t)(vd < 0xFFFFFFFFull ? vd : 0xFFFFFFFFull)};
+            const uint32_t nt = __popc(mask);
+            tail += nt < room ? nt : room;
+            emit(take && !local, v, vd);
+          });
     }
     for (uint32_t b = head; b < tail; b += 32) {
       const uint32_t k = b + lane;
       const bool t = k < tail;
-      emit(t, t ? Q[k] : 0u);
+      QEnt q{0, 0, 0};
+      if (t) q = Q[k];
+      emit(t, q.v, q.deg);
     }
     __syncwarp();
   }
@@ -512,8 +581,8 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
     }
     if (nv) {
       ProfScope ps(g, F_REACH_VGC);
-      k_reach_vgc<kReachBlock, kVgcQueue>
-          <<<grid_for(g, v_items * 32, kReachBlock), kReachBlock, 0, g->stream>>>(vg[0], vg[1], tau);
+      k_reach_vgc<kVgcBlock, kVgcQueue>
+          <<<grid_for(g, v_items * 32, kVgcBlock), kVgcBlock, 0, g->stream>>>(vg[0], vg[1], tau);
     }
     if (np) {
       ProfScope ps(g, F_REACH_PUSH);

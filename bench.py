@@ -231,6 +231,22 @@ def run_reference(args, world, rank, dist) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_ncu_step(args) -> None:
+    """Profiling target: build the workload, upload it, run one warm-up solve
+    and one solve, and nothing else (no CPU baseline, no end-to-end pass)."""
+    import psc
+
+    wl = WORKLOADS[args.workload]
+    g = wl["make"](psc)
+    with psc.DeviceGraph(g) as dg:
+        params = psc.default_params(seed=1)
+        for _ in range(2):
+            dg.scc(params)
+        st = dg.stats()
+        log(f"ncu step: {args.workload} n={g.n} m={g.m} {st.total_ms:.2f} ms, "
+            f"{st.kernel_launches} launches")
+
+
 def run_gpu(args, world, rank, local, dist) -> None:
     import psc
     from psc import _lib
@@ -370,10 +386,15 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="knn")
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-step", action="store_true",
+                    help="profiling target: one warm-up solve and one solve only")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "psc":
         log("note: fewer than 3 warm-up steps")
     world, rank, local, dist = dist_setup()
+    if args.ncu_step:
+        run_ncu_step(args)
+        return
     try:
         if args.impl == "reference":
             run_reference(args, world, rank, dist)

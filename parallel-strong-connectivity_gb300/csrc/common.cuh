@@ -166,6 +166,9 @@ enum Buf : int {
   } while (0)
 
 int cuda_status(cudaError_t e);
+// Round tracing to stderr when the environment sets PSC_TRACE (the reference
+// prints per-round frontier sizes under DEBUG, src/reach.hpp:218-239).
+bool trace_on();
 void set_last_cuda_error(cudaError_t e);
 
 // Returns a device pointer of at least `bytes` for slot `b` (contents of a
@@ -233,6 +236,30 @@ __device__ __forceinline__ unsigned long long warp_append(unsigned long long* co
   return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// Warp-aggregated append of a batch: lane's values vals[k] with bit k of tm
+// set are written to consecutive slots of out claimed with one atomicAdd on
+// *counter for the whole warp.  Every lane of the warp calls it.
+template <int K, class T>
+__device__ __forceinline__ void warp_append_batch(uint32_t tm, const T* vals, T* out,
+                                                  unsigned long long* counter) {
+  const unsigned lane = lane_id();
+  const uint32_t cnt = __popc(tm);
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  if (total == 0) return;
+  unsigned long long base = 0;
+  if (lane == 31) base = atomicAdd(counter, (unsigned long long)total);
+  base = __shfl_sync(kFull, base, 31) + (incl - cnt);
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (tm & (1u << k)) out[base++] = vals[k];
+}
+
 // Warp sum of a u64 value.
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 #pragma unroll
@@ -244,6 +271,7 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 struct WarpExpandSmem {
   uint32_t excl[32];
   uint64_t beg[32];
+  uint32_t fail;  // per-source-lane failure bits (multi-search)
 };
 
 // Balanced edge expansion over the 32 lanes' adjacency ranges [beg, beg+deg):

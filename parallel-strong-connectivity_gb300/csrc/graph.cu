@@ -1,6 +1,7 @@
 // Handle lifecycle, scratch buffers, counters, profiling and graph upload
 // for libpsc_cuda.so.  Declared in include/psc.h.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "common.cuh"
@@ -17,6 +18,14 @@ const char* const kFamilyName[F_COUNT] = {
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+
+bool trace_on() {
+  static const bool on = [] {
+    const char* v = std::getenv("PSC_TRACE");
+    return v && *v && *v != '0';
+  }();
+  return on;
+}
 
 int cuda_status(cudaError_t e) {
   g_last_cuda = e;

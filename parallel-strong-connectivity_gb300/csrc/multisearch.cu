@@ -28,6 +28,7 @@
 // again, finding the pairs it already placed.  This replaces the reference's
 // restart of the whole search (scc.hpp:263-272) with the same fixed point.
 #include <algorithm>
+#include <cstdio>
 
 #include "common.cuh"
 #include "engines.cuh"
@@ -113,7 +114,8 @@ __device__ __forceinline__ int table_insert_from(unsigned long long* T, uint64_t
 // labels[w] == src.sub[s].  DIRECT: the first probe is an atomicCAS (one
 // round trip, for latency-bound rounds); otherwise a load, then a CAS only on
 // an empty slot.  PF: also load w's adjacency range.  A failed insert sets bit
-// s of src.fail.  emit(take, w, lab, vbeg, vdeg) is warp-collective.
+// s of src.fail.  emit(tm, keys) gets the lane's K candidate pairs and the mask
+// of those newly inserted (warp-collective).
 template <int K, bool DIRECT, bool PF, class Emit>
 __device__ __forceinline__ void ms_expand_claim(WarpExpandSmem& sm, MsSrc& src, uint64_t beg,
                                                 uint32_t deg, const uint64_t* __restrict__ off,
@@ -179,10 +181,11 @@ __device__ __forceinline__ void ms_expand_claim(WarpExpandSmem& sm, MsSrc& src, 
           old[k] = __ldcg(&T[h[k]]);
       }
     }
+    uint32_t tm = 0;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-      int r = 0;
       if (key[k] != kEmpty) {
+        int r;
         probes++;
         if (DIRECT) {
           r = old[k] == kEmpty ? 1 : old[k] == key[k] ? 0
@@ -197,10 +200,11 @@ __device__ __forceinline__ void ms_expand_claim(WarpExpandSmem& sm, MsSrc& src, 
         } else {
           r = table_insert_from(T, mask, key[k], h[k], kProbeLimit - 1, &probes);
         }
+        if (r == 1) tm |= 1u << k;
         if (r < 0) atomicOr(&src.fail, 1u << sl[k]);
       }
-      if (base + k * 32 < total) emit(r == 1, w[k], src.lab[sl[k]], vb[k], ve[k] - vb[k]);
     }
+    emit(tm, key);
   }
   __syncwarp();
 }
@@ -282,9 +286,8 @@ __global__ void __launch_bounds__(BLOCK, 3)
     uint32_t probes = 0;
     ms_expand_claim<kMsExpandK, false, false>(
         sm[wid], src, beg, deg, S.off, S.E, labels, S.T, S.mask, probes,
-        [&](bool take, uint32_t w, uint32_t lab, uint64_t, uint64_t) {
-          unsigned long long pos = warp_append(&S.ctr->next, take);
-          if (take) S.Fout[pos] = ((uint64_t)w << 32) | lab;
+        [&](uint32_t tm, const uint64_t* keys) {
+          warp_append_batch<kMsExpandK>(tm, keys, S.Fout, &S.ctr->next);
         });
     (sd ? pr1 : pr0) += probes;
     __syncwarp();
@@ -305,27 +308,112 @@ struct MsQEnt {
   uint32_t deg;
 };
 
+// Claims of one batch for pivot lab inside subproblem sub: each candidate's
+// label and adjacency range are loaded together, then the first table probes
+// (atomicCAS) of all K candidates are issued before any is resolved.  Returns
+// the mask of new pairs; sets *failed if an insert gave up.
+template <int K>
+__device__ __forceinline__ uint32_t ms_vgc_claim(const uint32_t* w, uint64_t* vb, uint64_t* ve,
+                                                 uint64_t sub, uint32_t lab,
+                                                 const uint64_t* __restrict__ off,
+                                                 const uint64_t* __restrict__ labels,
+                                                 unsigned long long* T, uint64_t mask,
+                                                 uint32_t& probes, bool& failed) {
+  uint64_t key[K], old[K], h[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    key[k] = kEmpty;
+    vb[k] = ve[k] = 0;
+    if (w[k] != 0xFFFFFFFFu) {
+      const uint64_t lw = __ldg(&labels[w[k]]);
+      vb[k] = __ldg(&off[w[k]]);
+      ve[k] = __ldg(&off[w[k] + 1]);
+      if (lw == sub) key[k] = ((uint64_t)w[k] << 32) | lab;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    old[k] = kEmpty;
+    h[k] = 0;
+    if (key[k] != kEmpty) {
+      h[k] = hash64(key[k]) & mask;
+      old[k] = atomicCAS(&T[h[k]], (unsigned long long)kEmpty, (unsigned long long)key[k]);
+    }
+  }
+  uint32_t tm = 0;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (key[k] != kEmpty) {
+      probes++;
+      const int r = old[k] == kEmpty ? 1 : old[k] == key[k] ? 0
+                    : table_insert_from(T, mask, key[k], h[k], kProbeLimit - 1, &probes);
+      if (r == 1) tm |= 1u << k;
+      failed |= r < 0;
+    }
+  return tm;
+}
+
+// Places this lane's new pairs (bit k of tm) into the warp's queue while it
+// has room, then spills (w, lab) pairs: one warp scan, at most one atomic.
+template <int K>
+__device__ __forceinline__ void ms_vgc_place(uint32_t tm, const uint32_t* w, const uint64_t* vb,
+                                             const uint64_t* ve, uint32_t lab, MsQEnt* Q,
+                                             uint32_t& tail, uint32_t tq, uint64_t* Fout,
+                                             unsigned long long* next_ctr) {
+  const unsigned lane = lane_id();
+  const uint32_t cnt = __popc(tm);
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  if (total == 0) return;
+  const uint32_t room = tq - tail;
+  const uint32_t nloc = total < room ? total : room;
+  unsigned long long sbase = 0;
+  if (total > nloc && lane == 0) sbase = atomicAdd(next_ctr, (unsigned long long)(total - nloc));
+  sbase = __shfl_sync(kFull, sbase, 0);
+  uint32_t r = incl - cnt;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (tm & (1u << k)) {
+      if (r < nloc) {
+        const uint64_t vd = ve[k] - vb[k];
+        Q[tail + r] = MsQEnt{vb[k], w[k], (uint32_t)(vd < 0xFFFFFFFFull ? vd : 0xFFFFFFFFull)};
+      } else {
+        Fout[sbase + (r - nloc)] = ((uint64_t)w[k] << 32) | lab;
+      }
+      r++;
+    }
+  tail += nloc;
+  __syncwarp();
+}
+
 // VGC sub-round for up to two sides: one frontier pair (u, l) per warp.  If
 // 0 < deg(u) < tau the warp runs a local BFS for pivot l inside u's
-// subproblem in a shared-memory queue of tq = min(tau, QCAP) vertices: a
-// neighbour whose (w, l) insert succeeds stays in the queue while there is
-// room, else (w, l) spills to the next frontier.  Queued vertices with more
-// than tq out-edges and the queue's remainder spill too.  A queued vertex
-// whose expansion hit a failed insert is re-queued as a pair.
+// subproblem in a shared-memory queue of tq = min(tau, QCAP) vertices: each
+// wave offers l along the edges of up to 32 queued vertices (one vertex per
+// lane when their degrees are at most K, else the balanced expansion); a new
+// pair stays in the queue while there is room, else spills to the next
+// frontier.  Queued vertices with more than tq out-edges and the queue's
+// remainder spill too.  A queued vertex whose expansion hit a failed insert is
+// re-queued as a pair.
 template <int BLOCK, int QCAP>
 __global__ void __launch_bounds__(BLOCK)
     k_ms_vgc(MsSide s0, MsSide s1, const uint64_t* __restrict__ labels, uint32_t tau) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
-  __shared__ MsSrc ssrc[BLOCK / 32];
   __shared__ MsQEnt sq[BLOCK / 32][QCAP];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
   MsQEnt* Q = sq[wid];
-  MsSrc& src = ssrc[wid];
   unsigned long long sc0 = 0, sc1 = 0, rq0 = 0, rq1 = 0, ex0 = 0, ex1 = 0;
   uint32_t pr0 = 0, pr1 = 0;
+  if (lane == 0) sm[wid].fail = 0;
+  __syncwarp();
   for (uint64_t i = gw; i < s0.nin + s1.nin; i += nw) {
     const int sd = i < s0.nin ? 0 : 1;
     const MsSide S = sd ? s1 : s0;
@@ -340,8 +428,7 @@ __global__ void __launch_bounds__(BLOCK)
       if (take) S.Fout[pos] = ((uint64_t)w << 32) | lab;
     };
     if (lane == 0) (sd ? ex1 : ex0)++;
-    src.sub[lane] = sub;
-    src.lab[lane] = lab;
+    uint32_t probes = 0;
     if (!(du > 0 && du < tq)) {
       if (du > kHeavyDeg) {
         if (lane == 0) {
@@ -349,12 +436,10 @@ __global__ void __launch_bounds__(BLOCK)
           S.Fheavy[hh] = key;
           S.hflag[hh] = 0;
         }
-        __syncwarp();
         continue;
       }
       if (lane == 0) (sd ? sc1 : sc0) += du;
       bool failed = false;
-      uint32_t probes = 0;
       for (uint64_t b = ub; b < ue; b += 32) {
         const uint64_t e = b + lane;
         bool take = false;
@@ -395,35 +480,74 @@ __global__ void __launch_bounds__(BLOCK)
         if (lane > 0 || head > 0) (sd ? ex1 : ex0)++;
       }
       head += wave;
-      if (lane == 0) src.fail = 0;
       __syncwarp();
-      emit(spill_self, x);
+      if (__any_sync(kFull, spill_self)) emit(spill_self, x);
       (sd ? sc1 : sc0) += deg;
-      uint32_t probes = 0;
-      ms_expand_claim<kMsK, true, true>(
-          sm[wid], src, beg, deg, S.off, S.E, labels, S.T, S.mask, probes,
-          [&](bool take, uint32_t w, uint32_t, uint64_t vb, uint64_t vd) {
-            const unsigned m = __ballot_sync(kFull, take);
-            const uint32_t rank = __popc(m & ((1u << lane) - 1u));
-            const uint32_t room = tq - tail;
-            const bool local = take && rank < room;
-            if (local)
-              Q[tail + rank] = MsQEnt{vb, w, (uint32_t)(vd < 0xFFFFFFFFull ? vd : 0xFFFFFFFFull)};
-            const uint32_t nt = __popc(m);
-            tail += nt < room ? nt : room;
-            emit(take && !local, w);
-          });
+      bool failed = false;
+      uint32_t incl = deg;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      sm[wid].excl[lane] = incl - deg;
+      sm[wid].beg[lane] = beg;
+      __syncwarp();
+      for (uint32_t base = 0; base < total; base += 32 * kMsK) {
+        uint32_t w[kMsK];
+        int sl[kMsK];
+        uint64_t vb[kMsK], ve[kMsK];
+#pragma unroll
+        for (int k = 0; k < kMsK; k++) {
+          const uint32_t gi = base + k * 32 + lane;
+          w[k] = 0xFFFFFFFFu;
+          sl[k] = 0;
+          if (gi < total) {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+              int mid = (lo + hi + 1) >> 1;
+              if (sm[wid].excl[mid] <= gi)
+                lo = mid;
+              else
+                hi = mid - 1;
+            }
+            sl[k] = lo;
+            w[k] = __ldg(&S.E[sm[wid].beg[lo] + (gi - sm[wid].excl[lo])]);
+          }
+        }
+        bool fk = false;
+        const uint32_t tm = ms_vgc_claim<kMsK>(w, vb, ve, sub, lab, S.off, labels, S.T, S.mask,
+                                               probes, fk);
+        // a failure is charged to the source lane of the failed edge
+        if (fk) {
+#pragma unroll
+          for (int k = 0; k < kMsK; k++)
+            if (w[k] != 0xFFFFFFFFu) atomicOr(&sm[wid].fail, 1u << sl[k]);
+        }
+        ms_vgc_place<kMsK>(tm, w, vb, ve, lab, Q, tail, tq, S.Fout, &S.ctr->next);
+      }
+      __syncwarp();
+      failed = (sm[wid].fail >> lane) & 1u;
+      __syncwarp();
+      if (lane == 0) sm[wid].fail = 0;
+      __syncwarp();
       (sd ? pr1 : pr0) += probes;
-      __syncwarp();
-      const bool rq = (src.fail >> lane) & 1u;
-      emit(rq, x);
-      if (rq) (sd ? rq1 : rq0)++;
-      __syncwarp();
+      probes = 0;
+      const bool rq = failed && lane < wave;
+      if (__any_sync(kFull, rq)) {
+        emit(rq, x);
+        if (rq) (sd ? rq1 : rq0)++;
+      }
     }
-    for (uint32_t b = head; b < tail; b += 32) {
-      const uint32_t k = b + lane;
-      const bool t = k < tail;
-      emit(t, t ? Q[k].v : 0u);
+    // spill what is left in the queue with one reservation
+    const uint32_t rem = tail - head;
+    if (rem) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&S.ctr->next, (unsigned long long)rem);
+      base = __shfl_sync(kFull, base, 0);
+      for (uint32_t k = lane; k < rem; k += 32)
+        S.Fout[base + k] = ((uint64_t)Q[head + k].v << 32) | lab;
     }
     __syncwarp();
   }
@@ -626,6 +750,15 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
     }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(read_counters(g));
+    if (trace_on()) {
+      for (int k = 0; k < 2; k++)
+        if (st[k].nf)
+          std::fprintf(stderr, "ms side %d mode %s nf %llu next %llu edges %llu probes %llu cap %llu ne %llu\n",
+                       k, is_vgc[k] ? "vgc" : "expand", (unsigned long long)st[k].nf,
+                       g->hctr[st[k].cset].next, g->hctr[st[k].cset].edges,
+                       g->hctr[st[k].cset].probes, (unsigned long long)st[k].cap,
+                       (unsigned long long)st[k].ne);
+    }
     for (int k = 0; k < 2; k++) {
       MsState& s = st[k];
       if (s.nf == 0) continue;

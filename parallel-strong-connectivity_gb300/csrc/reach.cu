@@ -23,6 +23,7 @@
 // Expansion issues K edges per lane before using any of them, so the loads of
 // E and the claims on the bitmap overlap instead of forming one dependent
 // memory round trip per edge.
+#include <cstdio>
 #include <mutex>
 
 #include "common.cuh"
@@ -33,7 +34,8 @@ namespace psc {
 constexpr int kReachBlock = 256;
 constexpr int kVgcBlock = 128;  // VGC blocks: 4 warps
 constexpr int kVgcQueue = 512;  // VGC queue entries per warp (8 KB of 16-byte entries)
-constexpr int kExpandK = 8;     // edges in flight per lane
+constexpr int kExpandK = 8;     // VGC: edges in flight per lane
+constexpr int kPushK = 4;       // push: edges in flight per lane
 
 // One search side as the kernels see it.
 struct ReachSide {
@@ -65,10 +67,10 @@ __device__ __forceinline__ int find_src(const WarpExpandSmem& sm, uint32_t gi) {
 }
 
 // Balanced expansion of the 32 lanes' ranges [beg, beg+deg) with K edges per
-// lane in flight.  CHECK = read the bitmap word before the atomic (fewer
-// atomics when most targets are visited; one more round trip otherwise).
-// emit(take, v) is called by every lane (warp-collective).
-template <int K, bool CHECK, class Emit>
+// lane in flight: K loads of E, then a read of each target's bitmap word, then
+// atomicOr claims only for targets still unvisited.  emit(tm, v) gets the
+// lane's K candidates and the mask of those it claimed (warp-collective).
+template <int K, class Emit>
 __device__ __forceinline__ void expand_claim(WarpExpandSmem& sm, uint64_t beg, uint32_t deg,
                                              const uint32_t* __restrict__ E, uint32_t* vis,
                                              Emit&& emit) {
@@ -85,7 +87,7 @@ __device__ __forceinline__ void expand_claim(WarpExpandSmem& sm, uint64_t beg, u
   __syncwarp();
   for (uint32_t base = 0; base < total; base += 32 * K) {
     uint32_t v[K];
-    bool take[K];
+    uint32_t pre = 0, tm = 0;
 #pragma unroll
     for (int k = 0; k < K; k++) {
       const uint32_t gi = base + k * 32 + lane;
@@ -96,22 +98,15 @@ __device__ __forceinline__ void expand_claim(WarpExpandSmem& sm, uint64_t beg, u
       }
     }
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-      take[k] = false;
-      if (v[k] != 0xFFFFFFFFu) {
-        const uint32_t b = 1u << (v[k] & 31);
-        if (!CHECK || !(__ldcg(&vis[v[k] >> 5]) & b)) take[k] = true;
-      }
-    }
+    for (int k = 0; k < K; k++)
+      if (v[k] != 0xFFFFFFFFu && !(__ldcg(&vis[v[k] >> 5]) & (1u << (v[k] & 31)))) pre |= 1u << k;
 #pragma unroll
     for (int k = 0; k < K; k++)
-      if (take[k]) {
+      if (pre & (1u << k)) {
         const uint32_t b = 1u << (v[k] & 31);
-        take[k] = !(atomicOr(&vis[v[k] >> 5], b) & b);
+        if (!(atomicOr(&vis[v[k] >> 5], b) & b)) tm |= 1u << k;
       }
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (base + k * 32 < total) emit(take[k], v[k]);
+    emit(tm, v);
   }
   __syncwarp();
 }
@@ -167,72 +162,14 @@ __global__ void __launch_bounds__(BLOCK) k_reach_push(ReachSide s0, ReachSide s1
       deg = (uint32_t)d;
     }
     (sd ? scanned1 : scanned0) += deg;
-    expand_claim<kExpandK, true>(sm[wid], beg, deg, S.E, S.vis, [&](bool take, uint32_t v) {
-      unsigned long long pos = warp_append(&S.ctr->next, take);
-      if (take) {
-        S.qout[pos] = v;
-        (sd ? nedges1 : nedges0) += S.off[v + 1] - S.off[v];
-      }
+    expand_claim<kPushK>(sm[wid], beg, deg, S.E, S.vis, [&](uint32_t tm, const uint32_t* v) {
+      warp_append_batch<kPushK>(tm, v, S.qout, &S.ctr->next);
+#pragma unroll
+      for (int k = 0; k < kPushK; k++)
+        if (tm & (1u << k)) (sd ? nedges1 : nedges0) += S.off[v[k] + 1] - S.off[v[k]];
     });
   }
   flush_side_counters(s0.ctr, s1.ctr, scanned0, scanned1, nedges0, nedges1, exp0, exp1);
-}
-
-// Like expand_claim without the pre-check, and each candidate's adjacency
-// range off[v], off[v+1] is loaded alongside its claim (speculatively: the
-// load is wasted when the claim fails), so a claimed vertex enters the local
-// queue with its range and the next wave needs no dependent offset load.
-// emit(take, v, vbeg, vdeg) is warp-collective.
-template <int K, class Emit>
-__device__ __forceinline__ void expand_claim_pf(WarpExpandSmem& sm, uint64_t beg, uint32_t deg,
-                                                const uint64_t* __restrict__ off,
-                                                const uint32_t* __restrict__ E, uint32_t* vis,
-                                                Emit&& emit) {
-  const unsigned lane = lane_id();
-  uint32_t incl = deg;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(kFull, incl, o);
-    if ((int)lane >= o) incl += t;
-  }
-  const uint32_t total = __shfl_sync(kFull, incl, 31);
-  sm.excl[lane] = incl - deg;
-  sm.beg[lane] = beg;
-  __syncwarp();
-  for (uint32_t base = 0; base < total; base += 32 * K) {
-    uint32_t v[K];
-    uint64_t vb[K], ve[K];
-    bool take[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-      const uint32_t gi = base + k * 32 + lane;
-      v[k] = 0xFFFFFFFFu;
-      if (gi < total) {
-        const int s = find_src(sm, gi);
-        v[k] = __ldg(&E[sm.beg[s] + (gi - sm.excl[s])]);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-      vb[k] = ve[k] = 0;
-      if (v[k] != 0xFFFFFFFFu) {
-        vb[k] = __ldg(&off[v[k]]);
-        ve[k] = __ldg(&off[v[k] + 1]);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-      take[k] = false;
-      if (v[k] != 0xFFFFFFFFu) {
-        const uint32_t b = 1u << (v[k] & 31);
-        take[k] = !(atomicOr(&vis[v[k] >> 5], b) & b);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (base + k * 32 < total) emit(take[k], v[k], vb[k], ve[k] - vb[k]);
-  }
-  __syncwarp();
 }
 
 // Local-queue entry: a claimed vertex with its adjacency range.
@@ -242,13 +179,78 @@ struct QEnt {
   uint32_t deg;
 };
 
+// Places this lane's claimed candidates (bit k of tm <=> w[k] claimed) into the
+// warp's local queue while it has room, then spills the rest to the global
+// frontier: one warp scan and at most one global atomic for the whole warp.
+template <int K>
+__device__ __forceinline__ void vgc_place(uint32_t tm, const uint32_t* w, const uint64_t* vb,
+                                          const uint64_t* ve, QEnt* Q, uint32_t& tail, uint32_t tq,
+                                          uint32_t* qout, unsigned long long* next_ctr,
+                                          unsigned long long& nedges) {
+  const unsigned lane = lane_id();
+  const uint32_t cnt = __popc(tm);
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  if (total == 0) return;
+  const uint32_t room = tq - tail;
+  const uint32_t nloc = total < room ? total : room;
+  unsigned long long sbase = 0;
+  if (total > nloc && lane == 0) sbase = atomicAdd(next_ctr, (unsigned long long)(total - nloc));
+  sbase = __shfl_sync(kFull, sbase, 0);
+  uint32_t r = incl - cnt;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (tm & (1u << k)) {
+      const uint64_t vd = ve[k] - vb[k];
+      if (r < nloc) {
+        Q[tail + r] = QEnt{vb[k], w[k], (uint32_t)(vd < 0xFFFFFFFFull ? vd : 0xFFFFFFFFull)};
+      } else {
+        qout[sbase + (r - nloc)] = w[k];
+        nedges += vd;
+      }
+      r++;
+    }
+  tail += nloc;
+  __syncwarp();
+}
+
+// Claims of one batch: each candidate's adjacency range is loaded alongside
+// its claim (speculatively: wasted when the claim fails), so a claimed vertex
+// enters the queue with its range and the next wave needs no dependent load.
+template <int K>
+__device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, uint64_t* ve,
+                                              const uint64_t* __restrict__ off, uint32_t* vis) {
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    vb[k] = ve[k] = 0;
+    if (w[k] != 0xFFFFFFFFu) {
+      vb[k] = __ldg(&off[w[k]]);
+      ve[k] = __ldg(&off[w[k] + 1]);
+    }
+  }
+  uint32_t tm = 0;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (w[k] != 0xFFFFFFFFu) {
+      const uint32_t b = 1u << (w[k] & 31);
+      if (!(atomicOr(&vis[w[k] >> 5], b) & b)) tm |= 1u << k;
+    }
+  return tm;
+}
+
 // VGC round for up to two sides: one frontier vertex per warp.  A vertex with
 // 0 < deg < tau starts a local BFS in a shared-memory queue of tq =
-// min(tau, QCAP) entries: the warp expands up to 32 queued vertices per wave,
-// claims neighbours on the bitmap, and keeps a claimed vertex in the queue
-// while it has room, else spills it to the next frontier.  Queued vertices
-// with more than tq out-edges, and whatever is left in the queue when it
-// fills, are spilled too.  Other frontier vertices are expanded directly
+// min(tau, QCAP) entries: each wave takes up to 32 queued vertices and claims
+// their neighbours on the bitmap (one vertex per lane when all their degrees
+// are at most K, else the balanced expansion), keeping claimed vertices in the
+// queue while it has room and spilling the rest to the next frontier.  Queued
+// vertices with more than tq out-edges, and whatever is left in the queue when
+// it fills, are spilled too.  Other frontier vertices are expanded directly
 // (heavy ones by the whole grid).
 template <int BLOCK, int QCAP>
 __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau) {
@@ -263,13 +265,7 @@ __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1,
   for (uint64_t i = gw; i < s0.nin + s1.nin; i += nw) {
     const int sd = i < s0.nin ? 0 : 1;
     const ReachSide S = sd ? s1 : s0;
-    auto emit = [&](bool take, uint32_t v, uint64_t vdeg) {
-      unsigned long long pos = warp_append(&S.ctr->next, take);
-      if (take) {
-        S.qout[pos] = v;
-        (sd ? nedges1 : nedges0) += vdeg;
-      }
-    };
+    unsigned long long& nedges = sd ? nedges1 : nedges0;
     const uint32_t u = S.qin[sd ? i - s0.nin : i];
     const uint64_t ub = S.off[u], ue = S.off[u + 1];
     const uint64_t du = ue - ub;
@@ -288,7 +284,11 @@ __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1,
           v = __ldg(&S.E[e]);
           take = bit_set(S.vis, v);
         }
-        emit(take, v, take ? S.off[v + 1] - S.off[v] : 0);
+        unsigned long long pos = warp_append(&S.ctr->next, take);
+        if (take) {
+          S.qout[pos] = v;
+          nedges += S.off[v + 1] - S.off[v];
+        }
       }
       continue;
     }
@@ -314,26 +314,52 @@ __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1,
       }
       head += wave;
       __syncwarp();
-      emit(spill_self, x, xdeg);
+      if (__any_sync(kFull, spill_self)) {
+        unsigned long long pos = warp_append(&S.ctr->next, spill_self);
+        if (spill_self) {
+          S.qout[pos] = x;
+          nedges += xdeg;
+        }
+      }
       (sd ? scanned1 : scanned0) += deg;
-      expand_claim_pf<kExpandK>(
-          sm[wid], beg, deg, S.off, S.E, S.vis, [&](bool take, uint32_t v, uint64_t vb, uint64_t vd) {
-            const unsigned mask = __ballot_sync(kFull, take);
-            const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
-            const uint32_t room = tq - tail;
-            const bool local = take && rank < room;
-            if (local) Q[tail + rank] = QEnt{vb, v, (uint32_t)(vd < 0xFFFFFFFFull ? vd : 0xFFFFFFFFull)};
-            const uint32_t nt = __popc(mask);
-            tail += nt < room ? nt : room;
-            emit(take && !local, v, vd);
-          });
+      // balanced expansion over the wave's edges, 32*K per batch
+      uint32_t incl = deg;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      sm[wid].excl[lane] = incl - deg;
+      sm[wid].beg[lane] = beg;
+      __syncwarp();
+      for (uint32_t base = 0; base < total; base += 32 * kExpandK) {
+        uint32_t w[kExpandK];
+        uint64_t vb[kExpandK], ve[kExpandK];
+#pragma unroll
+        for (int k = 0; k < kExpandK; k++) {
+          const uint32_t gi = base + k * 32 + lane;
+          w[k] = 0xFFFFFFFFu;
+          if (gi < total) {
+            const int src = find_src(sm[wid], gi);
+            w[k] = __ldg(&S.E[sm[wid].beg[src] + (gi - sm[wid].excl[src])]);
+          }
+        }
+        const uint32_t tm = vgc_claim<kExpandK>(w, vb, ve, S.off, S.vis);
+        vgc_place<kExpandK>(tm, w, vb, ve, Q, tail, tq, S.qout, &S.ctr->next, nedges);
+      }
     }
-    for (uint32_t b = head; b < tail; b += 32) {
-      const uint32_t k = b + lane;
-      const bool t = k < tail;
-      QEnt q{0, 0, 0};
-      if (t) q = Q[k];
-      emit(t, q.v, q.deg);
+    // spill what is left in the queue with one reservation
+    const uint32_t rem = tail - head;
+    if (rem) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&S.ctr->next, (unsigned long long)rem);
+      base = __shfl_sync(kFull, base, 0);
+      for (uint32_t k = lane; k < rem; k += 32) {
+        const QEnt q = Q[head + k];
+        S.qout[base + k] = q.v;
+        nedges += q.deg;
+      }
     }
     __syncwarp();
   }
@@ -603,7 +629,24 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           (uint32_t*)g->bufs[s.slot_fb].p, n, g->ctr + s.cset);
     }
     PSC_CUDA(cudaGetLastError());
+    cudaEvent_t tr_b = nullptr;
+    const bool tr = trace_on();
+    if (tr) {
+      tr_b = take_event(g);
+      PSC_CUDA(cudaEventRecord(tr_b, g->stream));
+    }
     PSC_TRY(read_counters(g));
+    if (tr) {
+      float us = 0;  // ms since the start of the call
+      cudaEventElapsedTime(&us, g->t0, tr_b);
+      give_event(g, tr_b);
+      for (int k = 0; k < ns; k++)
+        if (mode[k] != M_NONE)
+          std::fprintf(stderr, "reach side %d round %u mode %s nf %llu next %llu edges %llu t %.3f ms\n",
+                       k, sides[k].rounds, mode[k] == M_VGC ? "vgc" : mode[k] == M_PUSH ? "push" : "pull",
+                       (unsigned long long)sides[k].nf, g->hctr[sides[k].cset].next,
+                       g->hctr[sides[k].cset].edges, us);
+    }
     for (int k = 0; k < ns; k++) {
       Side& s = sides[k];
       if (mode[k] == M_NONE) continue;

@@ -86,6 +86,17 @@ int psc_scc_device(psc_graph_t g, const psc_params_t* p, uint64_t* d_labels);
 int psc_reach(psc_graph_t g, uint32_t src, int dir, int local, uint32_t tau, uint8_t* dst_out,
               uint32_t* rounds);
 
+/* Connectivity (src/Connectivity.h:37-119) on a symmetric graph (upload with
+ * in_off = in_E = NULL, or any graph whose transpose equals itself): an LDD
+ * with parameter beta (0.2 in the reference CLI) then hook-and-compress
+ * union-find.  labels_out: host u32[n], each vertex's component root (a vertex
+ * id of the component).  If forest_out is non-NULL it receives a spanning
+ * forest as n_forest (u, v) edge pairs (u32[2*(n-1)] suffices; the reference's
+ * spanning_forest option, Connectivity.h:99-117); forest_out and n_forest are
+ * both NULL or both non-NULL. */
+int psc_cc(psc_graph_t g, double beta, uint32_t* labels_out, uint32_t* forest_out,
+           uint64_t* n_forest);
+
 /* psc_reach without any memory allocation.  No counterpart in the reference.
  *
  * For callers that may not allocate device memory themselves: engines that

@@ -1,0 +1,493 @@
+// Connectivity on the device (src/Connectivity.h:37-119): a low-diameter
+// decomposition followed by union-find over the edges that leave the largest
+// cluster.  The input graph is symmetric (as the reference requires).
+//
+// LDD (src/ldd.hpp:325-417) as an exponential-shift multi-source BFS: 1024
+// candidate centres hash32(1024 + i) % n are fixed up front; round r adds the
+// next floor(exp(r * beta)) of them that are still unlabelled, and every round
+// grows all clusters by one hop — a frontier vertex u offers label[u] to its
+// neighbours, and atomicCAS(label[v], NONE, label[u]) lets the first offer
+// win (the reference's compare_and_swap, ldd.hpp:226,253).  Rounds switch
+// between push (queue) and pull (bitmap) by the reference's rule.  Vertices
+// no cluster reaches are their own centre.
+//
+// Union-find (union_find_rules.h) as hook-and-compress: parent = LDD label;
+// for every vertex outside the most frequent cluster (get_max_label,
+// Connectivity.h:13-35, 10^4 hashed samples), every edge runs the lock-free
+// unite: find both roots with path halving, link the larger root under the
+// smaller with atomicCAS, retry on contention.  A final pass compresses every
+// vertex to its root.  Spanning forest: the LDD tree edges (v, parent[v]) plus
+// the edges whose unite linked two trees (Connectivity.h:99-117).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "engines.cuh"
+#include "scan.cuh"
+
+namespace psc {
+
+constexpr int kCcBlock = 256;
+constexpr int kLddSamples = 1024;   // ldd.hpp:462
+constexpr int kMaxLabelSamples = 10000;  // Connectivity.h:14
+
+__global__ void k_cc_init(uint32_t* label, uint32_t* parent, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    label[i] = kNone;
+    if (parent) parent[i] = (uint32_t)i;
+  }
+}
+
+// New centres perm[start .. start+count): claim the unlabelled ones and add
+// them to the frontier (queue, or bitmap in pull mode).
+__global__ void k_ldd_centres(const uint32_t* __restrict__ perm, uint32_t start, uint32_t count,
+                              uint32_t* label, uint32_t* q, uint32_t* fb, Counters* ctr) {
+  const unsigned lane = lane_id();
+  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < count;
+       base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + lane;
+    bool take = false;
+    uint32_t c = 0;
+    if (i < count) {
+      c = perm[start + i];
+      take = atomicCAS(&label[c], kNone, c) == kNone;
+    }
+    if (fb) {
+      if (take) atomicOr(&fb[c >> 5], 1u << (c & 31));
+      const unsigned m = __ballot_sync(kFull, take);
+      if (lane == 0 && m) atomicAdd(&ctr->next, (unsigned long long)__popc(m));
+    } else {
+      unsigned long long pos = warp_append(&ctr->next, take);
+      if (take) q[pos] = c;
+    }
+  }
+}
+
+// Push round: 32 frontier vertices per warp step, balanced expansion, K edges
+// in flight per lane; a neighbour is claimed with atomicCAS on its label.
+template <int BLOCK, int K>
+__global__ void __launch_bounds__(BLOCK)
+    k_ldd_push(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
+               const uint32_t* __restrict__ qin, uint64_t nin, uint32_t* label,
+               uint32_t* parent, uint32_t* qout, Counters* ctr) {
+  __shared__ WarpExpandSmem sm[BLOCK / 32];
+  __shared__ uint32_t s_lab[BLOCK];
+  __shared__ uint32_t s_u[BLOCK];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  unsigned long long scanned = 0, next_edges = 0;
+  for (uint64_t base = gw * 32; base < nin; base += nw * 32) {
+    const uint64_t i = base + lane;
+    uint64_t beg = 0, rem = 0;
+    uint32_t u = 0, lu = 0;
+    if (i < nin) {
+      u = qin[i];
+      beg = off[u];
+      rem = off[u + 1] - beg;
+      lu = label[u];
+    }
+    scanned += rem;
+    s_lab[wid * 32 + lane] = lu;
+    s_u[wid * 32 + lane] = u;
+    // adjacency lists in pieces of at most 2^26 edges (32-bit warp scan)
+    while (__any_sync(kFull, rem > 0)) {
+      const uint32_t deg = (uint32_t)(rem < (1ull << 26) ? rem : (1ull << 26));
+      uint32_t incl = deg;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      sm[wid].excl[lane] = incl - deg;
+      sm[wid].beg[lane] = beg;
+      __syncwarp();
+      for (uint32_t b = 0; b < total; b += 32 * K) {
+        uint32_t v[K], src[K], tm = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+          const uint32_t gi = b + k * 32 + lane;
+          v[k] = kNone;
+          src[k] = 0;
+          if (gi < total) {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (sm[wid].excl[mid] <= gi)
+                lo = mid;
+              else
+                hi = mid - 1;
+            }
+            src[k] = lo;
+            v[k] = __ldg(&E[sm[wid].beg[lo] + (gi - sm[wid].excl[lo])]);
+          }
+        }
+        uint32_t pre = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          if (v[k] != kNone && __ldcg(&label[v[k]]) == kNone) pre |= 1u << k;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          if (pre & (1u << k)) {
+            if (atomicCAS(&label[v[k]], kNone, s_lab[wid * 32 + src[k]]) == kNone) {
+              tm |= 1u << k;
+              if (parent) parent[v[k]] = s_u[wid * 32 + src[k]];
+            }
+          }
+        warp_append_batch<K>(tm, v, qout, &ctr->next);
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          if (tm & (1u << k)) next_edges += off[v[k] + 1] - off[v[k]];
+      }
+      __syncwarp();
+      beg += deg;
+      rem -= deg;
+    }
+  }
+  scanned = warp_sum(scanned);
+  next_edges = warp_sum(next_edges);
+  if (lane == 0) {
+    if (scanned) atomicAdd(&ctr->edges, scanned);
+    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
+  }
+}
+
+// Pull round (ldd.hpp:163-247): every unlabelled vertex takes the label of
+// its first neighbour in the frontier bitmap.  A warp owns 32 consecutive
+// vertices and writes their next-frontier word with one store.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_ldd_pull(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
+               const uint32_t* __restrict__ fb_in, uint32_t* label, uint32_t* parent,
+               uint32_t* fb_out, uint64_t n, Counters* ctr) {
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  const uint64_t nwords = (n + 31) >> 5;
+  unsigned long long cnt = 0, scanned = 0, next_edges = 0;
+  for (uint64_t w = gw; w < nwords; w += nw) {
+    const uint64_t v = w * 32 + lane;
+    bool found = false;
+    if (v < n && label[v] == kNone) {
+      const uint64_t b = off[v], e = off[v + 1];
+      uint64_t j = b;
+      for (; j < e; j++) {
+        const uint32_t x = __ldg(&E[j]);
+        if ((__ldg(&fb_in[x >> 5]) >> (x & 31)) & 1u) {
+          label[v] = label[x];
+          if (parent) parent[v] = x;
+          found = true;
+          break;
+        }
+      }
+      scanned += (found ? j + 1 : j) - b;
+      if (found) next_edges += e - b;
+    }
+    const uint32_t mask = __ballot_sync(kFull, found);
+    if (lane == 0) {
+      fb_out[w] = mask;
+      cnt += __popc(mask);
+    }
+  }
+  scanned = warp_sum(scanned);
+  next_edges = warp_sum(next_edges);
+  if (lane == 0) {
+    if (cnt) atomicAdd(&ctr->next, cnt);
+    if (scanned) atomicAdd(&ctr->edges, scanned);
+    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
+  }
+}
+
+__global__ void k_cc_queue_to_bitmap(const uint32_t* __restrict__ q, uint64_t nq, uint32_t* fb) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = q[i];
+    atomicOr(&fb[v >> 5], 1u << (v & 31));
+  }
+}
+
+__global__ void k_cc_bitmap_to_queue(const uint32_t* __restrict__ fb, uint64_t nwords, uint32_t* q,
+                                     Counters* ctr) {
+  const unsigned lane = lane_id();
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t base = gw * 32; base < nwords; base += nw * 32) {
+    const uint64_t w = base + lane;
+    uint32_t word = w < nwords ? fb[w] : 0u;
+    const uint32_t c = __popc(word);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(kFull, incl, o);
+      if ((int)lane >= o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    unsigned long long pos = 0;
+    if (lane == 0 && total) pos = atomicAdd(&ctr->aux0, (unsigned long long)total);
+    pos = __shfl_sync(kFull, pos, 0) + (incl - c);
+    while (word) {
+      const int b = __ffs(word) - 1;
+      word &= word - 1;
+      q[pos++] = (uint32_t)(w * 32 + b);
+    }
+  }
+}
+
+__global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+
+__global__ void k_ldd_finish(uint32_t* label, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    if (label[i] == kNone) label[i] = (uint32_t)i;
+}
+
+__global__ void k_sample_labels(const uint32_t* __restrict__ label, const uint32_t* __restrict__ idx,
+                                uint32_t count, uint32_t* out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    out[i] = label[idx[i]];
+}
+
+// find with path halving (union_find_rules.h:80-90, split/halve variants)
+__device__ __forceinline__ uint32_t uf_find(uint32_t* p, uint32_t x) {
+  uint32_t px = __ldcg(&p[x]);
+  while (px != x) {
+    const uint32_t gx = __ldcg(&p[px]);
+    if (gx != px) atomicCAS(&p[x], px, gx);
+    x = px;
+    px = gx;
+  }
+  return x;
+}
+
+// Unite over the edges of every vertex whose root is not the largest
+// cluster's (Connectivity.h:74-93).  Link the larger root under the smaller
+// (UniteRemCAS links high -> low, union_find_rules.h:193-225).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_uf_edges(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E, uint64_t n,
+               uint32_t* parent, uint32_t max_root, uint32_t* forest, Counters* ctr) {
+  __shared__ WarpExpandSmem sm[BLOCK / 32];
+  __shared__ uint32_t s_u[BLOCK];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  unsigned long long scanned = 0;
+  for (uint64_t base = gw * 32; base < n; base += nw * 32) {
+    const uint64_t i = base + lane;
+    uint64_t beg = 0, rem = 0;
+    if (i < n && uf_find(parent, (uint32_t)i) != max_root) {
+      beg = off[i];
+      rem = off[i + 1] - beg;
+    }
+    scanned += rem;
+    s_u[wid * 32 + lane] = (uint32_t)i;
+    // adjacency lists in pieces of at most 2^26 edges (32-bit warp scan)
+    while (__any_sync(kFull, rem > 0)) {
+      const uint32_t piece = (uint32_t)(rem < (1ull << 26) ? rem : (1ull << 26));
+      warp_expand(sm[wid], beg, piece, [&](bool act, int s, uint64_t e) {
+        bool linked = false;
+        uint32_t x = 0, y = 0;
+        if (act) {
+          x = s_u[wid * 32 + s];
+          y = __ldg(&E[e]);
+          for (;;) {
+            uint32_t rx = uf_find(parent, x), ry = uf_find(parent, y);
+            if (rx == ry) break;
+            if (rx < ry) {
+              const uint32_t t = rx;
+              rx = ry;
+              ry = t;
+            }
+            if (atomicCAS(&parent[rx], rx, ry) == rx) {
+              linked = true;
+              break;
+            }
+          }
+        }
+        if (forest) {
+          const unsigned long long pos = warp_append(&ctr->aux1, linked);
+          if (linked) {
+            forest[2 * pos] = x;
+            forest[2 * pos + 1] = y;
+          }
+        }
+      });
+      beg += piece;
+      rem -= piece;
+    }
+    __syncwarp();
+  }
+  scanned = warp_sum(scanned);
+  if (lane == 0 && scanned) atomicAdd(&ctr->edges, scanned);
+}
+
+__global__ void k_uf_final(uint32_t* parent, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    parent[i] = uf_find(parent, (uint32_t)i);
+}
+
+// LDD tree edges (v, parent[v]) for v != parent[v], appended to the forest.
+__global__ void k_ldd_tree_edges(const uint32_t* __restrict__ tree, uint64_t n, uint32_t* forest,
+                                 Counters* ctr) {
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
+       base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = base + lane_id();
+    const bool t = i < n && tree[i] != (uint32_t)i;
+    const unsigned long long pos = warp_append(&ctr->aux1, t);
+    if (t) {
+      forest[2 * pos] = (uint32_t)i;
+      forest[2 * pos + 1] = tree[i];
+    }
+  }
+}
+
+int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, uint64_t* n_forest) {
+  const uint64_t n = g->n, m = g->m, nwords = (n + 31) / 32;
+  const unsigned tb = kCcBlock;
+  uint32_t *qa, *qb, *fa, *fb, *perm, *tree = nullptr, *samp_idx, *samp;
+  PSC_TRY(ensure_t(g, B_QA, n + kLddSamples + 1, &qa));
+  PSC_TRY(ensure_t(g, B_QB, n + kLddSamples + 1, &qb));
+  PSC_TRY(ensure_t(g, B_FB_A, nwords + 1, &fa));
+  PSC_TRY(ensure_t(g, B_FB_B, nwords + 1, &fb));
+  PSC_TRY(ensure_t(g, B_AUX2, kLddSamples + 2 * kMaxLabelSamples, &perm));
+  samp_idx = perm + kLddSamples;
+  samp = samp_idx + kMaxLabelSamples;
+  if (d_forest) PSC_TRY(ensure_t(g, B_TMP32, n + 1, &tree));
+  // centres and label samples, hashed on the host (ldd.hpp:463-466,
+  // Connectivity.h:16-20)
+  std::vector<uint32_t> hp(kLddSamples + kMaxLabelSamples);
+  for (int i = 0; i < kLddSamples; i++) hp[i] = (uint32_t)(hash32(kLddSamples + i) % n);
+  const uint64_t seed = hash64(n + 1);
+  for (int i = 0; i < kMaxLabelSamples; i++) hp[kLddSamples + i] = (uint32_t)(hash64(i + seed) % n);
+  PSC_CUDA(cudaMemcpyAsync(perm, hp.data(), hp.size() * 4, cudaMemcpyHostToDevice, g->stream));
+  {
+    ProfScope ps(g, F_CC);
+    k_cc_init<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, tree, n);
+  }
+  const uint64_t threshold = m / 20;
+  uint64_t nf = 0, nf_edges = 0;
+  uint32_t sampled = 0, round = 0;
+  bool pull = false;
+  while (nf > 0 || sampled < (uint32_t)kLddSamples) {
+    round++;
+    if (round > n + kLddSamples + 2) return PSC_ERR_ITER_LIMIT;
+    const double stepf = std::floor(std::exp((double)round * beta));
+    const uint32_t work = (uint32_t)std::min<double>(stepf, (double)(kLddSamples - sampled));
+    if (work > 0) {
+      // new centres join the frontier: appended after the nf queued vertices
+      // (counter block 1 is the queue cursor) or set in the frontier bitmap
+      PSC_TRY(zero_counters(g));
+      k_set_u64<<<1, 1, 0, g->stream>>>(&g->ctr[1].next, pull ? 0ull : (unsigned long long)nf);
+      ProfScope ps(g, F_CC);
+      k_ldd_centres<<<grid_for(g, work, 256), 256, 0, g->stream>>>(perm, sampled, work, d_label,
+                                                                   pull ? nullptr : qa,
+                                                                   pull ? fa : nullptr, g->ctr + 1);
+      sampled += work;
+      PSC_TRY(read_counters(g));
+      nf = pull ? nf + g->hctr[1].next : g->hctr[1].next;
+    }
+    if (nf == 0) continue;
+    const bool want_pull = (nf + nf_edges) >= threshold;
+    if (want_pull && !pull) {
+      PSC_CUDA(cudaMemsetAsync(fa, 0, nwords * 4, g->stream));
+      k_cc_queue_to_bitmap<<<grid_for(g, nf, 256), 256, 0, g->stream>>>(qa, nf, fa);
+      pull = true;
+    } else if (!want_pull && pull) {
+      PSC_TRY(zero_counters(g));
+      k_cc_bitmap_to_queue<<<grid_for(g, nwords, 256), 256, 0, g->stream>>>(fa, nwords, qa, g->ctr);
+      pull = false;
+    }
+    PSC_TRY(zero_counters(g));
+    if (!pull) {
+      ProfScope ps(g, F_CC);
+      k_ldd_push<kCcBlock, 4><<<grid_for(g, nf, tb), tb, 0, g->stream>>>(
+          g->off, g->E, qa, nf, d_label, tree, qb, g->ctr);
+      std::swap(qa, qb);
+      swap_bufs(g, B_QA, B_QB);
+    } else {
+      ProfScope ps(g, F_CC);
+      k_ldd_pull<kCcBlock><<<grid_for(g, nwords * 32, tb), tb, 0, g->stream>>>(
+          g->off, g->E, fa, d_label, tree, fb, n, g->ctr);
+      std::swap(fa, fb);
+      swap_bufs(g, B_FB_A, B_FB_B);
+    }
+    PSC_CUDA(cudaGetLastError());
+    PSC_TRY(read_counters(g));
+    nf = g->hctr[0].next;
+    nf_edges = g->hctr[0].next_edges;
+  }
+  g->stats.reach_rounds = round;
+  {
+    ProfScope ps(g, F_CC);
+    k_ldd_finish<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, n);
+    k_sample_labels<<<grid_for(g, kMaxLabelSamples, 256), 256, 0, g->stream>>>(
+        d_label, samp_idx, kMaxLabelSamples, samp);
+  }
+  // most frequent sampled label (Connectivity.h:21-33): ties go to the
+  // smallest label, as the reference's scan of the sorted samples does
+  std::vector<uint32_t> hs(kMaxLabelSamples);
+  PSC_CUDA(cudaMemcpyAsync(hs.data(), samp, kMaxLabelSamples * 4, cudaMemcpyDeviceToHost,
+                           g->stream));
+  PSC_CUDA(cudaStreamSynchronize(g->stream));
+  std::sort(hs.begin(), hs.end());
+  uint32_t max_label = 0, max_cnt = 0;
+  for (size_t i = 0; i < hs.size();) {
+    size_t j = 1;
+    while (i + j < hs.size() && hs[i + j] == hs[i]) j++;
+    if (j > max_cnt) {
+      max_cnt = (uint32_t)j;
+      max_label = hs[i];
+    }
+    i += j;
+  }
+  // LDD labels are centre ids and every centre labels itself, so the label
+  // array is already a depth-1 union-find forest; max_label is its own root.
+  PSC_TRY(zero_counters(g));
+  uint32_t* forest = d_forest;
+  if (forest) {
+    ProfScope ps(g, F_CC);
+    k_ldd_tree_edges<<<grid_for(g, n, 256), 256, 0, g->stream>>>(tree, n, forest, g->ctr);
+  }
+  {
+    ProfScope ps(g, F_CC);
+    k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(g->off, g->E, n, d_label,
+                                                                   max_label, forest, g->ctr);
+  }
+  {
+    ProfScope ps(g, F_CC);
+    k_uf_final<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, n);
+  }
+  PSC_CUDA(cudaGetLastError());
+  if (n_forest) {
+    PSC_TRY(read_counters(g));
+    *n_forest = g->hctr[0].aux1;
+  }
+  return PSC_OK;
+}
+
+}  // namespace psc
+
+using namespace psc;
+
+extern "C" int psc_cc(psc_graph_t g, double beta, uint32_t* labels_out, uint32_t* forest_out,
+                      uint64_t* n_forest) {
+  if (!g || !labels_out || !(beta > 0)) return PSC_ERR_INVALID;
+  if ((forest_out == nullptr) != (n_forest == nullptr)) return PSC_ERR_INVALID;
+  PSC_TRY(call_begin(g));
+  uint32_t *d, *df = nullptr;
+  PSC_TRY(ensure_t(g, B_AUX0, g->n + 1, &d));
+  if (forest_out) PSC_TRY(ensure_t(g, B_AUX3, 2 * g->n + 2, &df));
+  uint64_t nfor = 0;
+  PSC_TRY(cc_run(g, beta, d, df, forest_out ? &nfor : nullptr));
+  PSC_CUDA(cudaMemcpyAsync(labels_out, d, g->n * 4, cudaMemcpyDeviceToHost, g->stream));
+  if (forest_out) {
+    *n_forest = nfor;
+    if (nfor) PSC_CUDA(cudaMemcpyAsync(forest_out, df, nfor * 8, cudaMemcpyDeviceToHost, g->stream));
+  }
+  return call_end(g);
+}

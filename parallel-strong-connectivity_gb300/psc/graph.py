@@ -228,6 +228,18 @@ class DeviceGraph:
         self.last_rounds = r.value
         return dst
 
+    def cc(self, beta: float = 0.2, forest: bool = False):
+        """Connected components of a symmetric graph: u32 root per vertex, and
+        with forest=True also a spanning forest as a (k, 2) u32 edge array."""
+        labels = np.empty(self.n, np.uint32)
+        if forest:
+            fo = np.empty(2 * max(self.n, 1), np.uint32)
+            k = C.c_uint64()
+            check(self._lib.psc_cc(self.h, beta, _ptr(labels), _ptr(fo), C.byref(k)), "psc_cc")
+            return labels, fo[: 2 * k.value].reshape(-1, 2)
+        check(self._lib.psc_cc(self.h, beta, _ptr(labels), None, None), "psc_cc")
+        return labels
+
     def stats(self) -> Stats:
         s = Stats()
         check(self._lib.psc_last_stats(self.h, C.byref(s)), "psc_last_stats")

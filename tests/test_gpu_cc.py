@@ -1,0 +1,78 @@
+"""GPU parity for Connectivity (LDD + union-find): the partition must equal
+the oracle's, scipy's (golden) and, with a spanning forest, the forest must
+span every component without a cycle."""
+import numpy as np
+import pytest
+
+import psc
+import pyoracle as O
+from _cases import GEN_CASES, generated, golden, golden_names, host_graph
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _dev(cuda_device):
+    return cuda_device
+
+
+def check_forest(n, labels_canon, forest):
+    """forest: (k, 2) edges.  Acyclic, inside components, k = n - #components."""
+    parent = np.arange(n)
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    for u, v in forest.tolist():
+        assert labels_canon[u] == labels_canon[v], "forest edge crosses components"
+        ru, rv = find(u), find(v)
+        assert ru != rv, "forest has a cycle"
+        parent[ru] = rv
+    ncomp = len(np.unique(labels_canon))
+    assert len(forest) == n - ncomp
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_cc_golden(name):
+    c = golden()[name]
+    s = host_graph(c).symmetrize()
+    with psc.DeviceGraph(s) as dg:
+        lab = dg.cc()
+        lab2, forest = dg.cc(forest=True)
+    assert np.array_equal(O.canon(lab), c["cc"])
+    assert np.array_equal(O.canon(lab2), c["cc"])
+    check_forest(s.n, c["cc"], forest)
+
+
+@pytest.mark.parametrize("kind,size,seed", GEN_CASES)
+def test_cc_generated(kind, size, seed):
+    s = generated(kind, size, seed).symmetrize()
+    ref = O.canon(O.cc(s.n, s.off, s.E))
+    with psc.DeviceGraph(s) as dg:
+        for beta in (0.2, 1.0):
+            assert np.array_equal(O.canon(dg.cc(beta)), ref)
+        lab, forest = dg.cc(forest=True)
+    assert np.array_equal(O.canon(lab), ref)
+    check_forest(s.n, ref, forest)
+
+
+def test_cc_many_components():
+    # disjoint cycles of various sizes plus isolated vertices
+    src, dst = [], []
+    n = 0
+    rng = np.random.default_rng(3)
+    for size in rng.integers(1, 40, 300).tolist():
+        for i in range(size):
+            src.append(n + i)
+            dst.append(n + (i + 1) % size)
+        n += size
+    g = psc.HostGraph.from_edges(n + 50, src, dst)
+    s = g.symmetrize()
+    with psc.DeviceGraph(s) as dg:
+        lab, forest = dg.cc(forest=True)
+    ref = O.canon(O.cc(s.n, s.off, s.E))
+    assert np.array_equal(O.canon(lab), ref)
+    check_forest(s.n, ref, forest)

@@ -86,6 +86,22 @@ int psc_scc_device(psc_graph_t g, const psc_params_t* p, uint64_t* d_labels);
 int psc_reach(psc_graph_t g, uint32_t src, int dir, int local, uint32_t tau, uint8_t* dst_out,
               uint32_t* rounds);
 
+/* BFS::bfs (src/bfs.hpp:200-238): dist_out host u32[n], hop distance from
+ * src along out-edges, UINT32_MAX = unreached.  *rounds (if non-NULL)
+ * receives the number of levels. */
+int psc_bfs(psc_graph_t g, uint32_t src, uint32_t* dist_out, uint32_t* rounds);
+
+/* LE_LIST::le_list (src/LeList.hpp:219-328) with the priority order supplied
+ * by the caller: perm[i] = vertex of priority i (u32[n], a permutation of
+ * [0, n); the reference draws it from parlay::random_permutation).  Distances
+ * follow out-edges (the reference runs it on symmetric graphs).  Output:
+ * triples (target, source vertex, distance), u32 each, sorted by (target,
+ * priority of the source) — the reference's list and seq_le_list's.  out holds
+ * cap triples (u32[3*cap]); *len receives the count.  If cap is too small,
+ * returns PSC_ERR_CAPACITY with *len = the required count. */
+int psc_lelist(psc_graph_t g, const uint32_t* perm, double beta, uint32_t* out, uint64_t cap,
+               uint64_t* len);
+
 /* Connectivity (src/Connectivity.h:37-119) on a symmetric graph (upload with
  * in_off = in_E = NULL, or any graph whose transpose equals itself): an LDD
  * with parameter beta (0.2 in the reference CLI) then hook-and-compress

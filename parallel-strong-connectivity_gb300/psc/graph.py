@@ -240,6 +240,29 @@ class DeviceGraph:
         check(self._lib.psc_cc(self.h, beta, _ptr(labels), None, None), "psc_cc")
         return labels
 
+    def bfs(self, src: int) -> np.ndarray:
+        """Hop distances from src (UINT32_MAX = unreached)."""
+        d = np.empty(self.n, np.uint32)
+        r = C.c_uint32()
+        check(self._lib.psc_bfs(self.h, src, _ptr(d), C.byref(r)), "psc_bfs")
+        self.last_rounds = r.value
+        return d
+
+    def lelist(self, perm: np.ndarray, beta: float = 1.5) -> np.ndarray:
+        """LE-lists for priority order perm: (k, 3) u32 triples (target,
+        source vertex, distance) sorted by (target, priority)."""
+        perm = np.ascontiguousarray(perm, dtype=np.uint32)
+        cap = max(16, 8 * self.n)
+        while True:
+            out = np.empty(3 * cap, np.uint32)
+            ln = C.c_uint64()
+            st = self._lib.psc_lelist(self.h, _ptr(perm), beta, _ptr(out), cap, C.byref(ln))
+            if st == _lib.PSC_ERR_CAPACITY:
+                cap = ln.value
+                continue
+            check(st, "psc_lelist")
+            return out[: 3 * ln.value].reshape(-1, 3)
+
     def stats(self) -> Stats:
         s = Stats()
         check(self._lib.psc_last_stats(self.h, C.byref(s)), "psc_last_stats")

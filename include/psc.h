@@ -113,6 +113,12 @@ int psc_lelist(psc_graph_t g, const uint32_t* perm, double beta, uint32_t* out, 
 int psc_cc(psc_graph_t g, double beta, uint32_t* labels_out, uint32_t* forest_out,
            uint64_t* n_forest);
 
+/* LDD::ldd (src/ldd.hpp:325-417) on a symmetric graph: label_out host u32[n]
+ * = the centre (a vertex id) whose cluster holds each vertex; parent_out
+ * (optional) host u32[n] = BFS-tree parent inside the cluster (parent[v] = v
+ * for centres), the reference's spanning_tree output. */
+int psc_ldd(psc_graph_t g, double beta, uint32_t* label_out, uint32_t* parent_out);
+
 /* psc_reach without any memory allocation.  No counterpart in the reference.
  *
  * For callers that may not allocate device memory themselves: engines that

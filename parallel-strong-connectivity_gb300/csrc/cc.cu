@@ -346,10 +346,11 @@ __global__ void k_ldd_tree_edges(const uint32_t* __restrict__ tree, uint64_t n, 
   }
 }
 
-int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, uint64_t* n_forest) {
+// LDD into d_label (centre ids); tree (optional) receives BFS parents.
+int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
   const uint64_t n = g->n, m = g->m, nwords = (n + 31) / 32;
   const unsigned tb = kCcBlock;
-  uint32_t *qa, *qb, *fa, *fb, *perm, *tree = nullptr, *samp_idx, *samp;
+  uint32_t *qa, *qb, *fa, *fb, *perm, *samp_idx, *samp;
   PSC_TRY(ensure_t(g, B_QA, n + kLddSamples + 1, &qa));
   PSC_TRY(ensure_t(g, B_QB, n + kLddSamples + 1, &qb));
   PSC_TRY(ensure_t(g, B_FB_A, nwords + 1, &fa));
@@ -357,7 +358,6 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
   PSC_TRY(ensure_t(g, B_AUX2, kLddSamples + 2 * kMaxLabelSamples, &perm));
   samp_idx = perm + kLddSamples;
   samp = samp_idx + kMaxLabelSamples;
-  if (d_forest) PSC_TRY(ensure_t(g, B_TMP32, n + 1, &tree));
   // centres and label samples, hashed on the host (ldd.hpp:463-466,
   // Connectivity.h:16-20)
   std::vector<uint32_t> hp(kLddSamples + kMaxLabelSamples);
@@ -428,6 +428,17 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
     k_sample_labels<<<grid_for(g, kMaxLabelSamples, 256), 256, 0, g->stream>>>(
         d_label, samp_idx, kMaxLabelSamples, samp);
   }
+  PSC_CUDA(cudaGetLastError());
+  return PSC_OK;
+}
+
+int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, uint64_t* n_forest) {
+  const uint64_t n = g->n;
+  const unsigned tb = kCcBlock;
+  uint32_t* tree = nullptr;
+  if (d_forest) PSC_TRY(ensure_t(g, B_TMP32, n + 1, &tree));
+  PSC_TRY(ldd_run(g, beta, d_label, tree));
+  uint32_t* samp = (uint32_t*)g->bufs[B_AUX2].p + kLddSamples + kMaxLabelSamples;
   // most frequent sampled label (Connectivity.h:21-33): ties go to the
   // smallest label, as the reference's scan of the sorted samples does
   std::vector<uint32_t> hs(kMaxLabelSamples);
@@ -489,5 +500,18 @@ extern "C" int psc_cc(psc_graph_t g, double beta, uint32_t* labels_out, uint32_t
     *n_forest = nfor;
     if (nfor) PSC_CUDA(cudaMemcpyAsync(forest_out, df, nfor * 8, cudaMemcpyDeviceToHost, g->stream));
   }
+  return call_end(g);
+}
+
+extern "C" int psc_ldd(psc_graph_t g, double beta, uint32_t* label_out, uint32_t* parent_out) {
+  if (!g || !label_out || !(beta > 0)) return PSC_ERR_INVALID;
+  PSC_TRY(call_begin(g));
+  uint32_t *d, *dp = nullptr;
+  PSC_TRY(ensure_t(g, B_AUX0, g->n + 1, &d));
+  if (parent_out) PSC_TRY(ensure_t(g, B_TMP32, g->n + 1, &dp));
+  PSC_TRY(ldd_run(g, beta, d, dp));
+  PSC_CUDA(cudaMemcpyAsync(label_out, d, g->n * 4, cudaMemcpyDeviceToHost, g->stream));
+  if (parent_out)
+    PSC_CUDA(cudaMemcpyAsync(parent_out, dp, g->n * 4, cudaMemcpyDeviceToHost, g->stream));
   return call_end(g);
 }

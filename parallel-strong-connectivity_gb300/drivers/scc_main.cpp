@@ -1,46 +1,16 @@
 // `scc` command-line driver: the flags and output lines of the reference's
 // src/scc.cpp:31-72 (so scripts that parse "average cost" keep working), over
 // the drop-in headers include/psc/scc.hpp.  Extra flag: -seed (pivot order).
-#include <sys/time.h>
-
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <string>
 
+#include "cli_common.hpp"
 #include "psc/graph.hpp"
 #include "psc/scc.hpp"
 
 namespace {
-
-struct CommandLine {  // src/parseCommandLine.hpp:4-37
-  int argc;
-  char** argv;
-  bool getOption(const std::string& o) const {
-    for (int i = 1; i < argc; i++)
-      if (o == argv[i]) return true;
-    return false;
-  }
-  const char* getOptionValue(const std::string& o) const {
-    for (int i = 1; i + 1 < argc; i++)
-      if (o == argv[i]) return argv[i + 1];
-    return nullptr;
-  }
-  long getOptionInt(const std::string& o, long d) const {
-    const char* s = getOptionValue(o);
-    return s ? std::atol(s) : d;
-  }
-  double getOptionDouble(const std::string& o, double d) const {
-    const char* s = getOptionValue(o);
-    return s ? std::atof(s) : d;
-  }
-};
-
-double now() {
-  timeval t;
-  gettimeofday(&t, nullptr);
-  return t.tv_sec + t.tv_usec / 1e6;
-}
 
 // src/scc.cpp:13-29
 void SCC_status(const psc::sequence<size_t>& label, size_t n) {
@@ -86,9 +56,9 @@ int main(int argc, char** argv) {
   SCC_P.timer_reset();
   double total = 0;
   for (int i = 0; i < repeat; i++) {
-    double t = now();
+    double t = wall_seconds();
     SCC_P.scc(label, beta, local_reach, local_scc);
-    double c = now() - t;
+    double c = wall_seconds() - t;
     total += c;
     std::cout << "scc cost: " << c << std::endl;
   }

@@ -240,6 +240,13 @@ class DeviceGraph:
         check(self._lib.psc_cc(self.h, beta, _ptr(labels), None, None), "psc_cc")
         return labels
 
+    def ldd(self, beta: float = 0.2) -> tuple[np.ndarray, np.ndarray]:
+        """Low-diameter decomposition: (centre label, BFS parent) per vertex."""
+        lab = np.empty(self.n, np.uint32)
+        par = np.empty(self.n, np.uint32)
+        check(self._lib.psc_ldd(self.h, beta, _ptr(lab), _ptr(par)), "psc_ldd")
+        return lab, par
+
     def bfs(self, src: int) -> np.ndarray:
         """Hop distances from src (UINT32_MAX = unreached)."""
         d = np.empty(self.n, np.uint32)

@@ -8,6 +8,10 @@ PROGRAM = r'''
 #include "psc/graph.hpp"
 #include "psc/scc.hpp"
 #include "psc/reach.hpp"
+#include "psc/bfs.hpp"
+#include "psc/ldd.hpp"
+#include "psc/Connectivity.h"
+#include "psc/LeList.hpp"
 int main(int argc, char** argv) {
   if (argc < 2) return 0;
   Graph graph = read_graph(argv[1]);
@@ -24,6 +28,17 @@ int main(int argc, char** argv) {
   R.swap_graph();
   R.reach(0, d2, true);
   R.swap_graph();
+  BFS B(graph);
+  parlay::sequence<NodeId> dist(graph.n);
+  B.bfs(0, dist);
+  auto cc = Connectivity(graph, 0.2);
+  auto cf = Connectivity(graph, 0.2, [](NodeId, NodeId) { return true; }, true);
+  LDD L(graph);
+  auto lp = L.ldd(0.2, true);
+  LE_LIST LE(graph);
+  LE.le_list(1.5);
+  LE.seq_le_list();
+  (void)cc; (void)cf; (void)lp;
   return (int)(label.size() != graph.n);
 }
 '''
@@ -43,5 +58,5 @@ def test_driver_built():
     exes = _drivers.build_drivers()
     for e in exes:
         assert e.exists()
-    out = subprocess.run([str(exes[0])], capture_output=True, text=True)
-    assert "usage: ./scc fileName" in out.stdout
+        out = subprocess.run([str(e)], capture_output=True, text=True)
+        assert f"usage: ./{e.name}" in out.stdout

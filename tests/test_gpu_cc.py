@@ -76,3 +76,24 @@ def test_cc_many_components():
     ref = O.canon(O.cc(s.n, s.off, s.E))
     assert np.array_equal(O.canon(lab), ref)
     check_forest(s.n, ref, forest)
+
+
+@pytest.mark.parametrize("kind,size,seed", [("knn", 20000, 3), ("rmat", 14, 2), ("grid", 128, 1)])
+def test_ldd_properties(kind, size, seed):
+    """LDD (src/ldd.hpp:325-417): every vertex carries a centre that labels
+    itself, BFS parents are neighbours in the same cluster, and clusters never
+    cross components."""
+    s = generated(kind, size, seed).symmetrize()
+    with psc.DeviceGraph(s) as dg:
+        lab, par = dg.ldd(0.2)
+    n = s.n
+    assert (lab < n).all()
+    assert (lab[lab] == lab).all(), "centres label themselves"
+    centres = lab == np.arange(n)
+    assert (par[centres] == np.arange(n)[centres]).all()
+    v = np.nonzero(~centres)[0]
+    assert (lab[par[v]] == lab[v]).all(), "parent in the same cluster"
+    for x in v[:2000].tolist():
+        assert par[x] in s.E[s.off[x]:s.off[x + 1]], "parent is a neighbour"
+    comp = O.canon(O.cc(n, s.off, s.E))
+    assert (comp[lab] == comp).all(), "clusters inside components"

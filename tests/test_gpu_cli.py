@@ -94,3 +94,33 @@ int main(int argc, char** argv) {
     assert np.array_equal(labels, O.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=6))
     assert np.array_equal(fw, O.reach_seq(g.n, g.off, g.E, 3))
     assert np.array_equal(bw, O.reach_seq(g.n, g.in_off, g.in_E, 3))
+
+
+def test_connectivity_and_lelist_drivers(tmp_path):
+    from psc import _drivers
+
+    exes = {e.name: e for e in _drivers.build_drivers()}
+    g = psc.HostGraph.knn(20000, 5, seed=21).symmetrize()
+    f = tmp_path / "knn_sym.bin"  # "sym" in the name: read as symmetric
+    g.write_bin(f)
+    lab_file = tmp_path / "cc.u32"
+    r = subprocess.run([str(exes["Connectivity"]), str(f), "-t", "2", "-labels", str(lab_file)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert re.search(r"^average_time: [0-9.e-]+$", r.stdout, re.M)
+    assert len(re.findall(r"^Connectivity time: ", r.stdout, re.M)) == 2
+    labels = np.fromfile(lab_file, dtype=np.uint32)
+    assert np.array_equal(O.canon(labels), O.canon(O.cc(g.n, g.off, g.E)))
+
+    small = psc.HostGraph.grid(30, 30, 0.3, seed=4).symmetrize()
+    f2 = tmp_path / "grid_sym.bin"
+    small.write_bin(f2)
+    out = tmp_path / "le.u32"
+    r = subprocess.run([str(exes["LeList"]), str(f2), "-t", "1", "-check", "-list", str(out)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "pass check" in r.stdout
+    assert re.search(r"^average cost: [0-9.e-]+$", r.stdout, re.M)
+    got = np.fromfile(out, dtype=np.uint32).reshape(-1, 3)
+    perm = psc.random_permutation(small.n, 4)  # le_seed default
+    assert np.array_equal(got, O.lelist_seq(small.n, small.off, small.E, perm))

@@ -119,6 +119,29 @@ int psc_cc(psc_graph_t g, double beta, uint32_t* labels_out, uint32_t* forest_ou
  * for centres), the reference's spanning_tree output. */
 int psc_ldd(psc_graph_t g, double beta, uint32_t* label_out, uint32_t* parent_out);
 
+/* Batches of independent graphs.  No counterpart in the reference, which
+ * solves one graph per call (src/scc.cpp:57-67).
+ *
+ * A batch is one uploaded graph that is the disjoint union of num_graphs
+ * graphs: graph k owns the vertex ids [vbase[k], vbase[k+1]) and all its edges
+ * (and transpose edges) stay inside that range.  psc_batch_set attaches the
+ * graph-offset table vbase (host u64[num_graphs+1], vbase[0] = 0,
+ * vbase[num_graphs] = n, nondecreasing) to the handle and checks every edge
+ * against it on the device: PSC_ERR_INVALID if one crosses two graphs. */
+int psc_batch_set(psc_graph_t g, const uint64_t* vbase, uint32_t num_graphs);
+uint32_t psc_batch_num_graphs(psc_graph_t g);
+/* SCC of every graph of the batch in one lockstep solve.  labels_out: host
+ * u64[n]; labels_out[vbase[k] + i] is vertex i's label in graph k, identical
+ * to psc_scc on graph k alone with the same parameters and with p->seed
+ * replaced by seeds[k] (seeds: host u64[num_graphs], or NULL for p->seed). */
+int psc_scc_batch(psc_graph_t g, const psc_params_t* p, const uint64_t* seeds, uint64_t* labels_out);
+int psc_scc_batch_device(psc_graph_t g, const psc_params_t* p, const uint64_t* seeds,
+                         uint64_t* d_labels);
+/* Connectivity of every graph of a batch of symmetric graphs: labels_out host
+ * u32[n], each vertex's component root as a vertex id local to its graph (the
+ * same partition as psc_cc on each graph alone). */
+int psc_cc_batch(psc_graph_t g, double beta, uint32_t* labels_out);
+
 /* psc_reach without any memory allocation.  No counterpart in the reference.
  *
  * For callers that may not allocate device memory themselves: engines that

@@ -77,6 +77,24 @@ const uint64_t* psc_hgraph_in_off(psc_hgraph_t g); /* NULL until built */
 const uint32_t* psc_hgraph_in_E(psc_hgraph_t g);
 void psc_hgraph_free(psc_hgraph_t g);
 
+/* Packs count graphs into one disjoint union for psc_batch_set: graph k's
+ * vertex i becomes vertex vbase_out[k] + i (vbase_out: u64[count+1]).  The
+ * transpose of every member is built if missing and packed too; the union is
+ * symmetric when every member is.  The members stay owned by the caller. */
+psc_hgraph_t psc_hgraph_pack(const psc_hgraph_t* graphs, uint32_t count, uint64_t* vbase_out);
+
+/* Seeded batch workload.  Member k uses seed seed0 + k and a size exponent u
+ * uniform in [log2_min, log2_max): even k is an R-MAT graph with
+ * 2^round(u) vertices, 16 * 2^round(u) draws and (a,b,c) = (0.57,0.19,0.19);
+ * odd k is a 2D kNN graph (k = 5) of floor(2^u) points.  spec returns
+ * kind 0 (R-MAT, size = log2 n) or 1 (kNN, size = points); 0 on success. */
+int psc_batch_member_spec(uint32_t k, uint64_t seed0, double log2_min, double log2_max,
+                          uint32_t* kind, uint64_t* size);
+psc_hgraph_t psc_hgraph_batch_member(uint32_t k, uint64_t seed0, double log2_min, double log2_max);
+/* Members 0..count-1 generated in parallel and packed (as psc_hgraph_pack). */
+psc_hgraph_t psc_hgraph_batch(uint32_t count, uint64_t seed0, double log2_min, double log2_max,
+                              uint64_t* vbase_out);
+
 /* out[i] = Feistel bijection of i on [0, n) keyed by seed. */
 void psc_random_permutation(uint64_t n, uint64_t seed, uint32_t* out);
 

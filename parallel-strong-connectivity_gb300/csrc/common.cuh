@@ -44,6 +44,7 @@ enum Family : int {
   F_CC,
   F_LE,
   F_TRANSPOSE,
+  F_BATCH,
   F_COUNT
 };
 extern const char* const kFamilyName[F_COUNT];
@@ -61,7 +62,9 @@ struct Counters {
   unsigned long long aux1;       // kernel-specific (re-queued pairs)
   unsigned long long expanded;   // vertices whose adjacency was read
   unsigned long long unvisited;  // vertices examined by a pull round
-  unsigned long long pad[6];
+  unsigned long long heavy_edges;  // edges scanned by the heavy-vertex kernels
+  unsigned long long heavy_probes; // table slots probed by the heavy-pair kernel
+  unsigned long long pad[4];
 };
 constexpr int kCounterSets = 4;
 
@@ -111,6 +114,11 @@ struct psc_graph_s {
   cudaEvent_t u0 = nullptr, u1 = nullptr;  // caller timer (psc_timer_*)
   cudaEvent_t ph[4] = {nullptr, nullptr, nullptr, nullptr};  // SCC phase marks
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> grow_events;  // table resizes
+  // graph-offset table of a batch of disjoint graphs (psc_batch_set)
+  uint32_t num_graphs = 0;
+  std::vector<uint64_t> vbase;     // host copy, num_graphs + 1 vertex bases
+  uint64_t* d_vbase = nullptr;     // device copy
+  uint32_t* d_gid = nullptr;       // u32[n] graph of each vertex
 };
 
 namespace psc {
@@ -149,6 +157,9 @@ enum Buf : int {
   B_AUX1,
   B_AUX2,
   B_AUX3,
+  B_GRAPHS,       // per-graph arrays of a batch
+  B_FLAB,         // u32 labels of a batch's pivots
+  B_SCHED,        // window schedule of a batch's prefix-doubling rounds
   B_COUNT
 };
 

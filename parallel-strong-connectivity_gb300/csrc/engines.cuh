@@ -21,19 +21,55 @@ int reach_run(psc_graph_s* g, uint32_t src, bool backward, bool local, uint32_t 
 int reach_pair(psc_graph_s* g, uint32_t src, bool local, uint32_t tau, uint32_t pull_div,
                uint32_t* vis_f, uint32_t* vis_b, uint32_t* rounds_f, uint32_t* rounds_b);
 
+// Forward and backward reachability from n_srcs device sources at once (the
+// first pivots of a batch of disjoint graphs share one search).
+int reach_pair_multi(psc_graph_s* g, const uint32_t* d_srcs, uint64_t n_srcs, bool local,
+                     uint32_t tau, uint32_t pull_div, uint32_t* vis_f, uint32_t* vis_b,
+                     uint32_t* rounds_f, uint32_t* rounds_b);
+
 // Multi-search (SCC::multi_search, src/scc.hpp:144-275) of one batch in both
 // directions at once: closure of the pivots front[i] (labels label_offset + i)
 // inside their subproblems, left in table slots B_TF (forward) and B_TB
 // (backward).  prev_ne: table sizes of the previous batch (sizing hint).
+// front_labels, when given, holds each pivot's label instead of
+// label_offset + i.
 struct MsResult {
   uint64_t cap = 0;  // table capacity (power of two)
   uint64_t ne = 0;   // entries
 };
 int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t label_offset,
             const uint64_t* labels, const psc_params_t* p, const uint64_t prev_ne[2],
-            MsResult out[2]);
+            MsResult out[2], const uint32_t* front_labels = nullptr);
+
+// Partition of one batch (src/scc.hpp:437-464): (v, l) in both tables left by
+// ms_pair -> labels[v] = max(l | TOP), else max(l).
+int scc_partition(psc_graph_s* g, const MsResult res[2], uint64_t* labels);
+
+// Runs phases(g) between the SCC phase events and fills stats.phase_ms
+// (trim, first pivot, multi-search, table growth).  phases records ph[1] and
+// ph[2] itself.
+template <class Phases>
+int scc_timed(psc_graph_s* g, Phases phases);
+int scc_phase_times(psc_graph_s* g);
+void scc_clear_grow_events(psc_graph_s* g);
+
+template <class Phases>
+int scc_timed(psc_graph_s* g, Phases phases) {
+  scc_clear_grow_events(g);
+  PSC_CUDA(cudaEventRecord(g->ph[0], g->stream));
+  PSC_TRY(phases(g));
+  return scc_phase_times(g);
+}
 
 // SCC into device labels (u64[n]).
 int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* d_labels);
+
+// SCC of every graph of a batch (graph-offset table set by psc_batch_set)
+// into device labels u64[n] holding each graph's own labels (vertex ids local
+// to the graph); seeds: per-graph pivot-order seeds (null: p->seed for all).
+int scc_batch_run(psc_graph_s* g, const psc_params_t* p, const uint64_t* seeds, uint64_t* d_labels);
+
+// Connectivity labels u32[n] of the union (cc.cu).
+int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, uint64_t* n_forest);
 
 }  // namespace psc

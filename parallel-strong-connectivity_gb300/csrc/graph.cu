@@ -13,7 +13,7 @@ namespace psc {
 const char* const kFamilyName[F_COUNT] = {
     "trim",        "reach_push", "reach_pull", "reach_vgc", "heavy",     "label_first",
     "compact",     "ms_seed",    "ms_expand",  "ms_vgc",    "table",     "partition",
-    "finalise",    "cc",         "lelist",     "transpose"};
+    "finalise",    "cc",         "lelist",     "transpose",  "batch"};
 
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 
@@ -319,6 +319,8 @@ int psc_graph_free(psc_graph_t g) {
   if (g->E) cudaFree(g->E);
   if (g->ctr) cudaFree(g->ctr);
   if (g->hctr) cudaFreeHost(g->hctr);
+  if (g->d_vbase) cudaFree(g->d_vbase);
+  if (g->d_gid) cudaFree(g->d_gid);
   for (auto& p : g->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);

@@ -505,6 +505,114 @@ const uint32_t* psc_hgraph_in_E(psc_hgraph_t g) {
 }
 void psc_hgraph_free(psc_hgraph_t g) { delete g; }
 
+psc_hgraph_t psc_hgraph_pack(const psc_hgraph_t* graphs, uint32_t count, uint64_t* vbase_out) {
+  if (!graphs || count == 0 || !vbase_out) {
+    set_err("pack needs at least one graph and a vbase array");
+    return nullptr;
+  }
+  std::vector<uint64_t> vb(count + 1, 0), eb(count + 1, 0);
+  bool sym = true;
+  for (uint32_t k = 0; k < count; k++) {
+    if (!graphs[k]) {
+      set_err("pack: null graph");
+      return nullptr;
+    }
+    vb[k + 1] = vb[k] + graphs[k]->n;
+    eb[k + 1] = eb[k] + graphs[k]->m;
+    sym = sym && graphs[k]->symmetric;
+  }
+  if (vb[count] >= 0xFFFFFFFFull) {
+    set_err("pack: more than 2^32-2 vertices");
+    return nullptr;
+  }
+  for (uint32_t k = 0; k < count; k++)
+    if (psc_hgraph_build_transpose(graphs[k]) != 0) return nullptr;
+  auto* p = new psc_hgraph_s();
+  p->n = vb[count];
+  p->m = eb[count];
+  p->off.resize(p->n + 1);
+  p->E.resize(p->m);
+  p->in_off.resize(p->n + 1);
+  p->in_E.resize(p->m);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < (int64_t)count; k++) {
+    const psc_hgraph_s* g = graphs[k];
+    const uint64_t v0 = vb[k], e0 = eb[k];
+    for (uint64_t i = 0; i < g->n; i++) {
+      p->off[v0 + i] = e0 + g->off[i];
+      p->in_off[v0 + i] = e0 + g->in_off[i];
+    }
+    for (uint64_t j = 0; j < g->m; j++) {
+      p->E[e0 + j] = (uint32_t)(v0 + g->E[j]);
+      p->in_E[e0 + j] = (uint32_t)(v0 + g->in_E[j]);
+    }
+  }
+  p->off[p->n] = p->m;
+  p->in_off[p->n] = p->m;
+  p->symmetric = sym;
+  p->has_transpose = true;
+  std::copy(vb.begin(), vb.end(), vbase_out);
+  return p;
+}
+
+// The batch workload: member k is seeded by seed0 + k; its size exponent u is
+// uniform in [log2_min, log2_max) (a log-uniform vertex count).  Even members
+// are R-MAT graphs with 2^round(u) vertices, 16 draws per vertex and
+// (a, b, c) = (0.57, 0.19, 0.19); odd members are 2D kNN graphs with
+// floor(2^u) points and k = 5.
+int psc_batch_member_spec(uint32_t k, uint64_t seed0, double log2_min, double log2_max,
+                          uint32_t* kind, uint64_t* size) {
+  if (!(log2_max >= log2_min) || log2_min < 1 || log2_max > 31) return -1;
+  const uint64_t seed = seed0 + k;
+  const double u = log2_min + (log2_max - log2_min) * psc::rng_unit(seed, 0);
+  if (k % 2 == 0) {
+    if (kind) *kind = 0;
+    if (size) *size = (uint64_t)std::llround(u);  // log2 of the vertex count
+  } else {
+    if (kind) *kind = 1;
+    if (size) *size = std::max<uint64_t>(6, (uint64_t)std::floor(std::exp2(u)));
+  }
+  return 0;
+}
+
+psc_hgraph_t psc_hgraph_batch_member(uint32_t k, uint64_t seed0, double log2_min, double log2_max) {
+  uint32_t kind = 0;
+  uint64_t size = 0;
+  if (psc_batch_member_spec(k, seed0, log2_min, log2_max, &kind, &size) != 0) {
+    set_err("batch member: log2 range must lie in [1, 31]");
+    return nullptr;
+  }
+  psc_hgraph_t g = kind == 0 ? psc_hgraph_rmat((uint32_t)size, 16ull << size, 0.57, 0.19, 0.19, seed0 + k)
+                             : psc_hgraph_knn(size, 5, seed0 + k);
+  if (g && psc_hgraph_build_transpose(g) != 0) {
+    delete g;
+    return nullptr;
+  }
+  return g;
+}
+
+psc_hgraph_t psc_hgraph_batch(uint32_t count, uint64_t seed0, double log2_min, double log2_max,
+                              uint64_t* vbase_out) {
+  if (count == 0 || !vbase_out) {
+    set_err("batch: count must be positive");
+    return nullptr;
+  }
+  std::vector<psc_hgraph_t> members(count, nullptr);
+  // members in parallel; each member's own parallel loops run on its thread
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < (int64_t)count; k++)
+    members[k] = psc_hgraph_batch_member((uint32_t)k, seed0, log2_min, log2_max);
+  psc_hgraph_t p = nullptr;
+  bool ok = true;
+  for (auto m : members) ok = ok && m != nullptr;
+  if (ok)
+    p = psc_hgraph_pack(members.data(), count, vbase_out);
+  else
+    set_err("batch: a member could not be generated");
+  for (auto m : members) delete m;
+  return p;
+}
+
 void psc_random_permutation(uint64_t n, uint64_t seed, uint32_t* out) {
   psc::FeistelKey f = psc::feistel_key(n, seed);
 #pragma omp parallel for schedule(static, 65536)

@@ -63,10 +63,12 @@ struct MsSrc {
 };
 
 __global__ void k_ms_seed(const uint32_t* __restrict__ front, uint64_t nf, uint64_t label_offset,
-                          unsigned long long* T, uint64_t mask, uint64_t* F) {
+                          const uint32_t* __restrict__ front_labels, unsigned long long* T,
+                          uint64_t mask, uint64_t* F) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t key = ((uint64_t)front[i] << 32) | (uint64_t)(uint32_t)(label_offset + i);
+    const uint32_t lab = front_labels ? front_labels[i] : (uint32_t)(label_offset + i);
+    uint64_t key = ((uint64_t)front[i] << 32) | (uint64_t)lab;
     uint32_t pr = 0;
     table_insert(T, mask, key, (uint32_t)(mask + 1 < 0xFFFFFFFFull ? mask + 1 : 0xFFFFFFFFu), &pr);
     F[i] = key;
@@ -604,8 +606,8 @@ __global__ void __launch_bounds__(BLOCK)
     requeued = warp_sum(requeued);
     unsigned long long pr = warp_sum((unsigned long long)probes);
     if (lane == 0) {
-      if (scanned) atomicAdd(&S.ctr->edges, scanned);
-      if (pr) atomicAdd(&S.ctr->probes, pr);
+      if (scanned) atomicAdd(&S.ctr->heavy_edges, scanned);
+      if (pr) atomicAdd(&S.ctr->heavy_probes, pr);
       if (requeued) {
         atomicAdd(&S.ctr->fail, requeued);
         atomicAdd(&S.ctr->aux1, requeued);
@@ -669,7 +671,7 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
 
 int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t label_offset,
             const uint64_t* labels, const psc_params_t* p, const uint64_t prev_ne[2],
-            MsResult out[2]) {
+            MsResult out[2], const uint32_t* front_labels) {
   const uint32_t tau = p->tau ? p->tau : 512;
   const bool local = p->local_scc != 0;
   const uint64_t vgc_limit = (uint64_t)g->num_sms * 32;
@@ -690,7 +692,8 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       ProfScope ps(g, F_MS_SEED);
       ps.bytes = 20.0 * n_front;
       k_ms_seed<<<grid_for(g, n_front, 256), 256, 0, g->stream>>>(
-          front, n_front, label_offset, (unsigned long long*)g->bufs[s.t_slot].p, s.cap - 1,
+          front, n_front, label_offset, front_labels, (unsigned long long*)g->bufs[s.t_slot].p,
+          s.cap - 1,
           (uint64_t*)g->bufs[s.a_slot].p);
     }
     s.nf = s.ne = n_front;
@@ -744,12 +747,24 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       k_ms_expand<kMsBlock><<<grid_for(g, e_items, kMsBlock), kMsBlock, 0, g->stream>>>(ex[0], ex[1],
                                                                                         labels);
     }
-    {
-      ProfScope ps(g, F_HEAVY);
-      k_ms_heavy<kMsBlock><<<g->num_sms * 4, kMsBlock, 0, g->stream>>>(hv[0], hv[1], labels);
-    }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(read_counters(g));
+    // Heavy pairs are rare: the grid-wide walk is launched only for a round
+    // that queued some, then the counters are read again.
+    if ((st[0].nf && g->hctr[st[0].cset].heavy) || (st[1].nf && g->hctr[st[1].cset].heavy)) {
+      {
+        ProfScope ps(g, F_HEAVY);
+        k_ms_heavy<kMsBlock><<<g->num_sms * 4, kMsBlock, 0, g->stream>>>(hv[0], hv[1], labels);
+      }
+      PSC_CUDA(cudaGetLastError());
+      PSC_TRY(read_counters(g));
+      if (g->profiling)
+        for (int k = 0; k < 2; k++)
+          if (st[k].nf) {
+            const Counters& c = g->hctr[st[k].cset];
+            g->prof[F_HEAVY].bytes += 24.0 * c.heavy + 12.0 * c.heavy_edges + 8.0 * c.heavy_probes;
+          }
+    }
     if (trace_on()) {
       for (int k = 0; k < 2; k++)
         if (st[k].nf)

@@ -54,6 +54,17 @@ __global__ void k_reach_init(uint32_t* vis, uint32_t* q, uint32_t src) {
   q[0] = src;
 }
 
+// Several sources at once (one per graph of a batch).
+__global__ void k_reach_init_multi(uint32_t* vis, uint32_t* q, const uint32_t* __restrict__ srcs,
+                                   uint64_t ns) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = srcs[i];
+    atomicOr(&vis[v >> 5], 1u << (v & 31));
+    q[i] = v;
+  }
+}
+
 __device__ __forceinline__ int find_src(const WarpExpandSmem& sm, uint32_t gi) {
   int lo = 0, hi = 31;
   while (lo < hi) {
@@ -400,7 +411,7 @@ __global__ void __launch_bounds__(BLOCK) k_reach_heavy(ReachSide s0, ReachSide s
     scanned = warp_sum(scanned);
     next_edges = warp_sum(next_edges);
     if (lane == 0) {
-      if (scanned) atomicAdd(&S.ctr->edges, scanned);
+      if (scanned) atomicAdd(&S.ctr->heavy_edges, scanned);
       if (next_edges) atomicAdd(&S.ctr->next_edges, next_edges);
     }
   }
@@ -541,9 +552,12 @@ Side make_side(bool backward, uint32_t* vis, int second) {
 
 }  // namespace
 
-// Runs the searches of `ns` sides (1 or 2) to completion.
+// Runs the searches of `ns` sides (1 or 2) to completion.  Side k starts from
+// srcs[k], or, when d_srcs is given, every side starts from the n_dsrc device
+// sources d_srcs.
 static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs, bool local,
-                       uint32_t tau, uint32_t pull_div) {
+                       uint32_t tau, uint32_t pull_div, const uint32_t* d_srcs = nullptr,
+                       uint64_t n_dsrc = 0) {
   const uint64_t n = g->n, nwords = (n + 31) / 32;
   // VGC rounds while the frontier is below one vertex per resident warp
   const uint64_t vgc_limit = (uint64_t)g->num_sms * 64;
@@ -558,8 +572,15 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
     PSC_TRY(ensure(g, s.slot_fb, (nwords + 1) * 4, &p));
     PSC_TRY(ensure(g, s.slot_heavy, (n + 1) * 4, &p));
     PSC_CUDA(cudaMemsetAsync(s.vis, 0, nwords * 4, g->stream));
-    k_reach_init<<<1, 1, 0, g->stream>>>(s.vis, (uint32_t*)g->bufs[s.slot_qa].p, srcs[k]);
-    s.nf = 1;
+    if (d_srcs) {
+      if (n_dsrc)
+        k_reach_init_multi<<<grid_for(g, n_dsrc, 256), 256, 0, g->stream>>>(
+            s.vis, (uint32_t*)g->bufs[s.slot_qa].p, d_srcs, n_dsrc);
+      s.nf = n_dsrc;
+    } else {
+      k_reach_init<<<1, 1, 0, g->stream>>>(s.vis, (uint32_t*)g->bufs[s.slot_qa].p, srcs[k]);
+      s.nf = 1;
+    }
     s.nf_edges = 0;
     s.pull = false;
     s.rounds = 0;
@@ -615,10 +636,6 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       k_reach_push<kReachBlock><<<grid_for(g, p_items, kReachBlock), kReachBlock, 0, g->stream>>>(
           pu[0], pu[1]);
     }
-    if (nh) {
-      ProfScope ps(g, F_HEAVY);
-      k_reach_heavy<kReachBlock><<<g->num_sms * 4, kReachBlock, 0, g->stream>>>(hv[0], hv[1]);
-    }
     for (int k = 0; k < ns; k++) {
       if (mode[k] != M_PULL) continue;
       Side& s = sides[k];
@@ -636,6 +653,23 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       PSC_CUDA(cudaEventRecord(tr_b, g->stream));
     }
     PSC_TRY(read_counters(g));
+    // Heavy vertices are rare: the grid-wide walk is launched only for a
+    // round that queued some, then the counters are read again.
+    bool heavy = false;
+    for (int k = 0; k < nh; k++) heavy |= g->hctr[hv[k].ctr - g->ctr].heavy != 0;
+    if (heavy) {
+      {
+        ProfScope ps(g, F_HEAVY);
+        k_reach_heavy<kReachBlock><<<g->num_sms * 4, kReachBlock, 0, g->stream>>>(hv[0], hv[1]);
+      }
+      PSC_CUDA(cudaGetLastError());
+      PSC_TRY(read_counters(g));
+      if (g->profiling)
+        for (int k = 0; k < nh; k++) {
+          const Counters& c = g->hctr[hv[k].ctr - g->ctr];
+          g->prof[F_HEAVY].bytes += 20.0 * c.heavy + 5.0 * c.heavy_edges;
+        }
+    }
     if (tr) {
       float us = 0;  // ms since the start of the call
       cudaEventElapsedTime(&us, g->t0, tr_b);
@@ -685,6 +719,16 @@ int reach_pair(psc_graph_s* g, uint32_t src, bool local, uint32_t tau, uint32_t 
   Side s[2] = {make_side(false, vis_f, 0), make_side(true, vis_b, 1)};
   const uint32_t srcs[2] = {src, src};
   PSC_TRY(reach_sides(g, s, 2, srcs, local, tau ? tau : 512, pull_div));
+  if (rounds_f) *rounds_f = s[0].rounds;
+  if (rounds_b) *rounds_b = s[1].rounds;
+  return PSC_OK;
+}
+
+int reach_pair_multi(psc_graph_s* g, const uint32_t* d_srcs, uint64_t n_srcs, bool local,
+                     uint32_t tau, uint32_t pull_div, uint32_t* vis_f, uint32_t* vis_b,
+                     uint32_t* rounds_f, uint32_t* rounds_b) {
+  Side s[2] = {make_side(false, vis_f, 0), make_side(true, vis_b, 1)};
+  PSC_TRY(reach_sides(g, s, 2, nullptr, local, tau ? tau : 512, pull_div, d_srcs, n_srcs));
   if (rounds_f) *rounds_f = s[0].rounds;
   if (rounds_b) *rounds_b = s[1].rounds;
   return PSC_OK;

@@ -79,9 +79,11 @@ __global__ void __launch_bounds__(kScanBlock) k_tile_emit(Value value, Emit emit
   }
 }
 
-// Host driver.  total may be null.
+// Host driver.  total may be null.  item_bytes / sel_bytes: algorithmic
+// bytes per input item and per selected item, for the profiling counters.
 template <class Value, class Emit>
-int scan_emit(psc_graph_s* g, uint64_t n, Value value, Emit emit, uint64_t* total, int fam = F_COMPACT) {
+int scan_emit(psc_graph_s* g, uint64_t n, Value value, Emit emit, uint64_t* total, int fam = F_COMPACT,
+              double item_bytes = 0, double sel_bytes = 0) {
   if (n == 0) {
     if (total) *total = 0;
     return PSC_OK;
@@ -108,7 +110,36 @@ int scan_emit(psc_graph_s* g, uint64_t n, Value value, Emit emit, uint64_t* tota
     PSC_CUDA(cudaStreamSynchronize(g->stream));
     *total = g->hctr->aux0;
   }
+  if (g->profiling) g->prof[fam].bytes += item_bytes * n + sel_bytes * (total ? *total : 0);
   return PSC_OK;
 }
+
+// Selections shared by the SCC drivers: in/out-degree-zero vertices
+// (src/scc.hpp:288-301), and live (not done) entries of a vertex list.
+struct ZeroFlag {
+  const uint64_t* off;
+  const uint64_t* in_off;
+  __device__ uint32_t operator()(uint64_t i) const {
+    return (off[i + 1] == off[i] || in_off[i + 1] == in_off[i]) ? 1u : 0u;
+  }
+};
+
+struct NotDoneAt {
+  const uint32_t* src;
+  const uint64_t* labels;
+  uint64_t base;
+  __device__ uint32_t operator()(uint64_t i) const {
+    return (labels[src[base + i]] & kTopBit) ? 0u : 1u;
+  }
+};
+
+struct CopyAt {
+  const uint32_t* src;
+  uint32_t* dst;
+  uint64_t base;
+  __device__ void operator()(uint64_t i, uint64_t excl, uint32_t v) const {
+    if (v) dst[excl] = src[base + i];
+  }
+};
 
 }  // namespace psc

@@ -29,14 +29,6 @@
 namespace psc {
 
 
-struct ZeroFlag {
-  const uint64_t* off;
-  const uint64_t* in_off;
-  __device__ uint32_t operator()(uint64_t i) const {
-    return (off[i + 1] == off[i] || in_off[i + 1] == in_off[i]) ? 1u : 0u;
-  }
-};
-
 struct TrimEmit {
   uint64_t* labels;
   uint32_t* nz;
@@ -47,24 +39,6 @@ struct TrimEmit {
       labels[i] = 0;
       nz[i - excl] = (uint32_t)i;
     }
-  }
-};
-
-struct NotDoneAt {
-  const uint32_t* src;
-  const uint64_t* labels;
-  uint64_t base;
-  __device__ uint32_t operator()(uint64_t i) const {
-    return (labels[src[base + i]] & kTopBit) ? 0u : 1u;
-  }
-};
-
-struct CopyAt {
-  const uint32_t* src;
-  uint32_t* dst;
-  uint64_t base;
-  __device__ void operator()(uint64_t i, uint64_t excl, uint32_t v) const {
-    if (v) dst[excl] = src[base + i];
   }
 };
 
@@ -123,14 +97,15 @@ __global__ void k_finalise(uint64_t* labels, uint64_t n) {
 
 static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p);
 
-int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
+void scc_clear_grow_events(psc_graph_s* g) {
   for (auto& pr : g->grow_events) {
     give_event(g, pr.first);
     give_event(g, pr.second);
   }
   g->grow_events.clear();
-  PSC_CUDA(cudaEventRecord(g->ph[0], g->stream));
-  PSC_TRY(scc_phases(g, labels, p));
+}
+
+int scc_phase_times(psc_graph_s* g) {
   PSC_CUDA(cudaEventSynchronize(g->ph[3]));
   float a = 0, b = 0, c = 0;
   PSC_CUDA(cudaEventElapsedTime(&a, g->ph[0], g->ph[1]));
@@ -149,6 +124,34 @@ int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
   return PSC_OK;
 }
 
+int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
+  return scc_timed(g, [&](psc_graph_s* h) { return scc_phases(h, labels, p); });
+}
+
+int scc_partition(psc_graph_s* g, const MsResult res[2], uint64_t* labels) {
+  const unsigned tb = 256;
+  const MsResult& rf = res[0];
+  const MsResult& rb = res[1];
+  const bool f_small = rf.cap <= rb.cap;
+  const unsigned long long* Ts = (const unsigned long long*)g->bufs[f_small ? B_TF : B_TB].p;
+  const unsigned long long* Tl = (const unsigned long long*)g->bufs[f_small ? B_TB : B_TF].p;
+  const uint64_t cap_s = f_small ? rf.cap : rb.cap, cap_l = f_small ? rb.cap : rf.cap;
+  {
+    ProfScope ps(g, F_PARTITION);
+    ps.bytes = 8.0 * cap_s + 16.0 * (f_small ? rf.ne : rb.ne);
+    k_partition_small<<<grid_for(g, cap_s, tb), tb, 0, g->stream>>>(Ts, cap_s, Tl, cap_l - 1,
+                                                                    (unsigned long long*)labels);
+  }
+  {
+    ProfScope ps(g, F_PARTITION);
+    ps.bytes = 8.0 * cap_l + 8.0 * (f_small ? rb.ne : rf.ne);
+    k_partition_large<<<grid_for(g, cap_l, tb), tb, 0, g->stream>>>(Tl, cap_l,
+                                                                    (unsigned long long*)labels);
+  }
+  PSC_CUDA(cudaGetLastError());
+  return PSC_OK;
+}
+
 static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
   const uint64_t n = g->n;
   const unsigned tb = 256;
@@ -157,11 +160,13 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
   PSC_TRY(ensure_t(g, B_TMP32, n + 1, &nz));
   // trim
   uint64_t n_zeros = 0;
-  PSC_TRY(scan_emit(g, n, ZeroFlag{g->off, g->in_off}, TrimEmit{labels, nz}, &n_zeros, F_TRIM));
+  // algorithmic bytes: 4 offsets read + one 8-byte label or 4-byte index written
+  PSC_TRY(scan_emit(g, n, ZeroFlag{g->off, g->in_off}, TrimEmit{labels, nz}, &n_zeros, F_TRIM, 40.0));
   const uint64_t np = n - n_zeros;
   if (np > 0) {
     FeistelKey key = feistel_key(np, p->seed);
     ProfScope ps(g, F_TRIM);
+    ps.bytes = 8.0 * np;
     k_perm_gather<<<grid_for(g, np, tb), tb, 0, g->stream>>>(nz, np, key, P);
   }
   uint64_t label_offset = n_zeros + 1;
@@ -184,7 +189,7 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
     }
     PSC_TRY(ensure_t(g, B_CENTERS, np + 1, &centers));
     uint64_t nc = 0;
-    PSC_TRY(scan_emit(g, np, NotDoneAt{P, labels, 0}, CopyAt{P, centers, 0}, &nc));
+    PSC_TRY(scan_emit(g, np, NotDoneAt{P, labels, 0}, CopyAt{P, centers, 0}, &nc, F_COMPACT, 12.0, 4.0));
     label_offset++;
     PSC_CUDA(cudaEventRecord(g->ph[2], g->stream));
 
@@ -202,35 +207,17 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
       if (step_size == 0) step_size = 1;
       uint64_t nf = 0;
       PSC_TRY(scan_emit(g, vs_size, NotDoneAt{centers, labels, cur_offset},
-                        CopyAt{centers, front, cur_offset}, &nf));
+                        CopyAt{centers, front, cur_offset}, &nf, F_COMPACT, 12.0, 4.0));
       cur_offset = end;
       if (nf == 0) continue;
       g->stats.batches++;
       MsResult res[2];
       const uint64_t prev[2] = {out_ne, in_ne};
       PSC_TRY(ms_pair(g, front, nf, label_offset, labels, p, prev, res));
-      const MsResult& rf = res[0];
-      const MsResult& rb = res[1];
       label_offset += nf;
-      const bool f_small = rf.cap <= rb.cap;
-      const unsigned long long* Ts = (const unsigned long long*)g->bufs[f_small ? B_TF : B_TB].p;
-      const unsigned long long* Tl = (const unsigned long long*)g->bufs[f_small ? B_TB : B_TF].p;
-      const uint64_t cap_s = f_small ? rf.cap : rb.cap, cap_l = f_small ? rb.cap : rf.cap;
-      {
-        ProfScope ps(g, F_PARTITION);
-        ps.bytes = 8.0 * cap_s + 16.0 * (f_small ? rf.ne : rb.ne);
-        k_partition_small<<<grid_for(g, cap_s, tb), tb, 0, g->stream>>>(
-            Ts, cap_s, Tl, cap_l - 1, (unsigned long long*)labels);
-      }
-      {
-        ProfScope ps(g, F_PARTITION);
-        ps.bytes = 8.0 * cap_l + 8.0 * (f_small ? rb.ne : rf.ne);
-        k_partition_large<<<grid_for(g, cap_l, tb), tb, 0, g->stream>>>(Tl, cap_l,
-                                                                        (unsigned long long*)labels);
-      }
-      PSC_CUDA(cudaGetLastError());
-      out_ne = rf.ne;
-      in_ne = rb.ne;
+      PSC_TRY(scc_partition(g, res, labels));
+      out_ne = res[0].ne;
+      in_ne = res[1].ne;
     }
   }
   if (np == 0) PSC_CUDA(cudaEventRecord(g->ph[2], g->stream));

@@ -5,4 +5,5 @@ ABI in include/psc.h); this package only loads it, builds inputs with
 libpsc_host.so and exposes the calls.  There is no CPU fallback.
 """
 from ._lib import Params, PscError, Stats, cuda, host, strerror  # noqa: F401
-from .graph import DeviceGraph, HostGraph, default_params, random_permutation  # noqa: F401
+from .graph import (DeviceGraph, HostGraph, batch_member, batch_member_spec,  # noqa: F401
+                    batch_workload, default_params, random_permutation)

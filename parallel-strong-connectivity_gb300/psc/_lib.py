@@ -83,6 +83,11 @@ CUDA_SIGNATURES = {
     "psc_ldd": (I32, [P, D, P, P]),
     "psc_lelist": (I32, [P, P, D, P, U64, C.POINTER(U64)]),
     "psc_reach_noalloc": (I32, [P, P, P, P, U64, U64, U32, I32, P, P, C.POINTER(U32)]),
+    "psc_batch_set": (I32, [P, P, U32]),
+    "psc_batch_num_graphs": (U32, [P]),
+    "psc_scc_batch": (I32, [P, C.POINTER(Params), P, P]),
+    "psc_scc_batch_device": (I32, [P, C.POINTER(Params), P, P]),
+    "psc_cc_batch": (I32, [P, D, P]),
     "psc_last_stats": (I32, [P, C.POINTER(Stats)]),
     "psc_set_profiling": (I32, [P, I32]),
     "psc_profile_count": (I32, []),
@@ -121,6 +126,10 @@ HOST_SIGNATURES = {
     "psc_hgraph_in_off": (P, [P]),
     "psc_hgraph_in_E": (P, [P]),
     "psc_hgraph_free": (None, [P]),
+    "psc_hgraph_pack": (P, [P, U32, P]),
+    "psc_batch_member_spec": (I32, [U32, U64, D, D, C.POINTER(U32), C.POINTER(U64)]),
+    "psc_hgraph_batch_member": (P, [U32, U64, D, D]),
+    "psc_hgraph_batch": (P, [U32, U64, D, D, P]),
     "psc_random_permutation": (None, [U64, U64, P]),
     "psc_host_last_error": (C.c_char_p, []),
 }

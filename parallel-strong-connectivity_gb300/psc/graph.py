@@ -131,6 +131,32 @@ class HostGraph:
         g.in_off, g.in_E = g.off, g.E
         return g
 
+    @staticmethod
+    def pack(graphs: list["HostGraph"]) -> tuple["HostGraph", np.ndarray]:
+        """Disjoint union of graphs for a batch: graph k's vertex i becomes
+        vbase[k] + i.  Returns (union, vbase u64[len(graphs)+1])."""
+        gs = [g.with_transpose() if not g.symmetric else g for g in graphs]
+        vb = np.zeros(len(gs) + 1, np.uint64)
+        eb = np.zeros(len(gs) + 1, np.uint64)
+        vb[1:] = np.cumsum([g.n for g in gs])
+        eb[1:] = np.cumsum([g.m for g in gs])
+
+        def cat(field_off, field_E):
+            off = np.concatenate([getattr(g, field_off)[:-1] + eb[k] for k, g in enumerate(gs)]
+                                 + [eb[-1:]]).astype(np.uint64)
+            E = np.concatenate([getattr(g, field_E).astype(np.uint64) + vb[k]
+                                for k, g in enumerate(gs)]).astype(np.uint32)
+            return off, E
+
+        off, E = cat("off", "E")
+        u = HostGraph(int(vb[-1]), int(eb[-1]), off, E)
+        if all(g.symmetric for g in gs):
+            u.symmetric = True
+            u.in_off, u.in_E = u.off, u.E
+        else:
+            u.in_off, u.in_E = cat("in_off", "in_E")
+        return u, vb
+
     def edge_list(self) -> tuple[np.ndarray, np.ndarray]:
         src = np.repeat(np.arange(self.n, dtype=np.uint32), np.diff(self.off).astype(np.int64))
         return src, self.E
@@ -142,6 +168,32 @@ def random_permutation(n: int, seed: int) -> np.ndarray:
     out = np.empty(n, dtype=np.uint32)
     _lib.host().psc_random_permutation(n, seed, _ptr(out))
     return out
+
+
+def batch_member_spec(k: int, seed0: int = 1000, log2_min: float = 8,
+                      log2_max: float = 18) -> tuple[str, int]:
+    """('rmat', log2 n) or ('knn', points) of member k of the batch workload."""
+    kind, size = C.c_uint32(), C.c_uint64()
+    if _lib.host().psc_batch_member_spec(k, seed0, log2_min, log2_max, C.byref(kind),
+                                         C.byref(size)) != 0:
+        raise ValueError("log2 range must lie in [1, 31]")
+    return ("rmat" if kind.value == 0 else "knn"), int(size.value)
+
+
+def batch_member(k: int, seed0: int = 1000, log2_min: float = 8,
+                 log2_max: float = 18) -> HostGraph:
+    """Member k of the seeded batch workload (with its transpose)."""
+    return HostGraph._adopt(_lib.host().psc_hgraph_batch_member(k, seed0, log2_min, log2_max),
+                            "batch_member")
+
+
+def batch_workload(count: int, seed0: int = 1000, log2_min: float = 8,
+                   log2_max: float = 18) -> tuple[HostGraph, np.ndarray]:
+    """Members 0..count-1 of the batch workload, generated in parallel and
+    packed: (union, vbase)."""
+    vb = np.zeros(count + 1, np.uint64)
+    h = _lib.host().psc_hgraph_batch(count, seed0, log2_min, log2_max, _ptr(vb))
+    return HostGraph._adopt(h, "batch_workload"), vb
 
 
 def default_params(**kw) -> Params:
@@ -213,6 +265,34 @@ class DeviceGraph:
         p = params or default_params()
         labels = out if out is not None else np.empty(self.n, np.uint64)
         check(self._lib.psc_scc(self.h, C.byref(p), _ptr(labels)), "psc_scc")
+        return labels
+
+    # -- batches of disjoint graphs -----------------------------------------
+    def set_batch(self, vbase: np.ndarray) -> None:
+        """Attach the graph-offset table of a packed batch (HostGraph.pack)."""
+        vb = np.ascontiguousarray(vbase, dtype=np.uint64)
+        check(self._lib.psc_batch_set(self.h, _ptr(vb), len(vb) - 1), "psc_batch_set")
+        self.vbase = vb
+
+    def scc_batch(self, params: Params | None = None, seeds=None,
+                  out: np.ndarray | None = None) -> np.ndarray:
+        """SCC labels of every graph of the batch, local to each graph."""
+        p = params or default_params()
+        sd = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.uint64)
+        labels = out if out is not None else np.empty(self.n, np.uint64)
+        check(self._lib.psc_scc_batch(self.h, C.byref(p), _ptr(sd), _ptr(labels)), "psc_scc_batch")
+        return labels
+
+    def scc_batch_device(self, d_labels: int, params: Params | None = None, seeds=None) -> None:
+        p = params or default_params()
+        sd = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.uint64)
+        check(self._lib.psc_scc_batch_device(self.h, C.byref(p), _ptr(sd), d_labels),
+              "psc_scc_batch_device")
+
+    def cc_batch(self, beta: float = 0.2) -> np.ndarray:
+        """Connectivity roots of every graph of a symmetric batch, local ids."""
+        labels = np.empty(self.n, np.uint32)
+        check(self._lib.psc_cc_batch(self.h, beta, _ptr(labels)), "psc_cc_batch")
         return labels
 
     def scc_device(self, d_labels: int, params: Params | None = None) -> None:

@@ -146,3 +146,53 @@ def test_adj_reader(tmp_path):
     assert np.array_equal(r.off, g.off) and np.array_equal(r.E, g.E)
     (tmp_path / "bad.adj").write_text("AdjacencyGraph\n5\n")
     assert not lib.psc_hgraph_read_adj(str(tmp_path / "bad.adj").encode())
+
+
+def test_batch_member_spec():
+    specs = [psc.batch_member_spec(k, 1000, 8, 18) for k in range(400)]
+    assert [s[0] for s in specs[:4]] == ["rmat", "knn", "rmat", "knn"]
+    for kind, size in specs:
+        if kind == "rmat":
+            assert 8 <= size <= 18
+        else:
+            assert 256 <= size < 1 << 18
+    # log-uniform: about half the kNN members lie below 2^13
+    knn = np.array([s for k, s in specs if k == "knn"])
+    assert 0.35 < np.mean(knn < 1 << 13) < 0.65
+    assert specs == [psc.batch_member_spec(k, 1000, 8, 18) for k in range(400)]
+    with pytest.raises(ValueError):
+        psc.batch_member_spec(0, 1, 5, 40)
+
+
+def test_batch_workload_is_packed_members():
+    count = 9
+    u, vb = psc.batch_workload(count, 11, 4, 10)
+    members = [psc.batch_member(k, 11, 4, 10) for k in range(count)]
+    assert len(vb) == count + 1 and vb[0] == 0 and vb[-1] == u.n
+    for k, m in enumerate(members):
+        kind, size = psc.batch_member_spec(k, 11, 4, 10)
+        assert m.n == (1 << size if kind == "rmat" else size)
+        assert int(vb[k + 1] - vb[k]) == m.n
+    p, pvb = psc.HostGraph.pack(members)
+    assert np.array_equal(pvb, vb)
+    for f in ("off", "E", "in_off", "in_E"):
+        assert np.array_equal(getattr(u, f), getattr(p, f)), f
+    # no edge leaves its member's id range
+    src, dst = u.edge_list()
+    gs = np.searchsorted(vb, src, side="right") - 1
+    assert ((dst >= vb[gs]) & (dst < vb[gs + 1])).all()
+    # transpose of the union = union of the transposes
+    t_off, t_E = O.transpose(u.n, u.off, u.E)
+    assert np.array_equal(t_off, u.in_off) and np.array_equal(t_E, u.in_E)
+
+
+def test_pack_symmetric_and_single():
+    a = psc.HostGraph.rmat(6, 300, seed=1).symmetrize()
+    b = psc.HostGraph.knn(50, 5, seed=2).symmetrize()
+    s, vb = psc.HostGraph.pack([a, b])
+    assert s.symmetric and s.in_E is s.E
+    assert list(vb) == [0, a.n, a.n + b.n]
+    one, vb1 = psc.HostGraph.pack([a])
+    assert np.array_equal(one.E, a.E) and list(vb1) == [0, a.n]
+    d, _ = psc.HostGraph.pack([a, psc.HostGraph.rmat(5, 100, seed=3)])
+    assert not d.symmetric and d.in_off is not None

@@ -198,8 +198,53 @@ def barrier(dist):
         dist.barrier()
 
 
+def run_reference_batch(args) -> None:
+    """Reference arm of the batch workload: the CPU restatement solves member
+    graphs one by one (as the reference's scc binary would, one graph per
+    run); each step is a stratified sample of 64 members."""
+    import psc
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    count = args.batch_count
+    stride = max(1, count // 64)
+    sample = list(range(0, count, stride))
+    members = [psc.batch_member(k, **BATCH) for k in sample]
+    threads = os.cpu_count() or 1
+
+    def step():
+        for k, mk in zip(sample, members):
+            pyoracle.scc(mk.n, mk.off, mk.E, mk.in_off, mk.in_E, seed=BATCH["seed0"] + k,
+                         nthreads=threads)
+
+    for _ in range(args.warmup):
+        step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t
+    value = len(sample) * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "batched SCC graphs/s", "value": value, "unit": "graphs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"scc_batch{count}", "graph": batch_desc(count), "graphs": count,
+                   "beta": 1.5, "tau": 512, "vgc": True},
+        "cpu_baseline": {"value": value, "unit": "graphs/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: {len(sample)} members (every {stride}th) solved "
+                                   "one by one by the OpenMP restatement of src/scc.hpp"},
+        "e2e": {"value": value, "unit": "graphs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, world, rank, dist) -> None:
     if rank != 0:
+        return
+    if args.workload == "batch":
+        run_reference_batch(args)
         return
     import psc
 
@@ -245,6 +290,206 @@ def run_ncu_step(args) -> None:
         st = dg.stats()
         log(f"ncu step: {args.workload} n={g.n} m={g.m} {st.total_ms:.2f} ms, "
             f"{st.kernel_launches} launches")
+
+
+BATCH = dict(seed0=1000, log2_min=8.0, log2_max=18.0)
+
+
+def batch_desc(count: int) -> str:
+    return (f"{count} directed graphs, vertex counts log-uniform in [2^8, 2^18); even members "
+            "R-MAT (16 draws per vertex, 0.57/0.19/0.19/0.05, dedup), odd members 2-D kNN k=5; "
+            "member k seeded 1000+k; packed into one CSR + transpose with a graph-offset table")
+
+
+def run_batch(args, world, rank, local, dist) -> None:
+    """Batched SCC: every step solves all graphs of the batch in one lockstep
+    call (psc_scc_batch_device); compared with per-graph plain solves of a
+    stratified sample of the same graphs on the same GPU."""
+    import psc
+    from psc import _lib
+
+    lib = psc.cuda()
+    if world > 1:
+        _lib.check(lib.psc_set_device(local), "psc_set_device")
+    if lib.psc_device_count() < 1:
+        raise SystemExit("no CUDA device")
+    count = args.batch_count
+    t = time.perf_counter()
+    g, vb = psc.batch_workload(count, **BATCH)
+    log(f"[rank {rank}] generated batch of {count}: n={g.n} m={g.m} in {time.perf_counter() - t:.1f}s")
+    n, m = g.n, g.m
+    seeds = (BATCH["seed0"] + np.arange(count)).astype(np.uint64)
+    params = psc.default_params()
+
+    pin = Pinned(lib)
+    h_off, h_E = pin.copy(g.off), pin.copy(g.E)
+    h_in_off, h_in_E = pin.copy(g.in_off), pin.copy(g.in_E)
+    h_labels = pin.empty(n, np.uint64)
+
+    dg = psc.DeviceGraph(g)
+    dg.set_batch(vb)
+    d_labels = C.c_void_p()
+    _lib.check(lib.psc_device_alloc(n * 8, C.byref(d_labels)), "psc_device_alloc")
+    for _ in range(args.warmup):
+        dg.scc_batch_device(d_labels.value, params, seeds)
+    ref_labels = dg.scc_batch(params, seeds)
+    chk = pin.empty(n, np.uint64)
+    _lib.check(lib.psc_copy(chk.ctypes.data, d_labels.value, n * 8), "psc_copy")
+    if not np.array_equal(chk, ref_labels):
+        raise SystemExit("device and host batched SCC outputs disagree")
+
+    barrier(dist)
+    launches = 0
+    with ClockSampler(local) as clk:
+        _lib.check(lib.psc_timer_start(dg.h), "psc_timer_start")
+        for _ in range(args.steps):
+            dg.scc_batch_device(d_labels.value, params, seeds)
+            launches += dg.stats().kernel_launches
+        ms = C.c_double()
+        _lib.check(lib.psc_timer_stop(dg.h, C.byref(ms)), "psc_timer_stop")
+    barrier(dist)
+    total_ms = max_over_ranks(dist, ms.value)
+    clocks = clk.summary()
+    value = count * args.steps * world / (total_ms / 1e3)
+    last = dg.stats()
+
+    dg.set_profiling(True)
+    dg.profile_reset()
+    for _ in range(args.profile_steps):
+        dg.scc_batch_device(d_labels.value, params, seeds)
+    prof = dg.profile()
+    dg.set_profiling(False)
+    roofline = roofline_of(prof, args.profile_steps)
+
+    # per-graph plain solves of a stratified sample (every stride-th member),
+    # each timed by CUDA events on its own handle, labels checked against the
+    # batch's
+    stride = max(1, count // args.plain_sample)
+    sample = list(range(0, count, stride))
+    plain_ms, plain_launches = 0.0, 0
+    mismatched = 0
+    for k in sample:
+        mk = g.member(vb, k)
+        pk = psc.default_params(seed=int(seeds[k]))
+        with psc.DeviceGraph(mk) as d1:
+            lab1 = d1.scc(pk)  # warm-up and check
+            if not np.array_equal(lab1, ref_labels[int(vb[k]):int(vb[k + 1])]):
+                mismatched += 1
+            d_l1 = C.c_void_p()
+            _lib.check(lib.psc_device_alloc(mk.n * 8, C.byref(d_l1)), "psc_device_alloc")
+            _lib.check(lib.psc_timer_start(d1.h), "psc_timer_start")
+            d1.scc_device(d_l1.value, pk)
+            t1 = C.c_double()
+            _lib.check(lib.psc_timer_stop(d1.h, C.byref(t1)), "psc_timer_stop")
+            plain_launches += d1.stats().kernel_launches
+            lib.psc_device_free(d_l1.value)
+        plain_ms += t1.value
+    if mismatched:
+        raise SystemExit(f"{mismatched} sampled graphs differ between batched and plain solves")
+    plain_rate = len(sample) / (plain_ms / 1e3)
+
+    # end to end: upload the packed batch from pinned memory, attach the
+    # graph-offset table, solve, read the labels back
+    h2d = h_off.nbytes + h_E.nbytes + h_in_off.nbytes + h_in_E.nbytes + vb.nbytes
+    d2h = n * 8
+    P = C.c_void_p
+    sd = np.ascontiguousarray(seeds)
+
+    def e2e_step():
+        h = P()
+        _lib.check(lib.psc_graph_upload(h_off.ctypes.data, h_E.ctypes.data, h_in_off.ctypes.data,
+                                        h_in_E.ctypes.data, n, m, C.byref(h)), "psc_graph_upload")
+        try:
+            _lib.check(lib.psc_batch_set(h, vb.ctypes.data, count), "psc_batch_set")
+            _lib.check(lib.psc_scc_batch(h, C.byref(params), sd.ctypes.data, h_labels.ctypes.data),
+                       "psc_scc_batch")
+        finally:
+            lib.psc_graph_free(h)
+
+    e2e_step()
+    if not np.array_equal(h_labels, ref_labels):
+        raise SystemExit("end-to-end batched SCC labels disagree")
+    barrier(dist)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t)
+    e2e_value = count * args.steps * world / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_batch(g, vb, seeds, sample)
+
+    lib.psc_device_free(d_labels.value)
+    dg.free()
+    pin.free()
+    if rank != 0:
+        return
+    line = {
+        "metric": "batched SCC graphs/s", "value": value, "unit": "graphs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic",
+        "config": {"workload": f"scc_batch{count}", "graph": batch_desc(count), "graphs": count,
+                   "n": n, "m": m, "beta": 1.5, "tau": 512, "vgc": True,
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)",
+                   "edges_per_s": m * args.steps * world / (total_ms / 1e3),
+                   "batches": last.batches, "subrounds": last.subrounds,
+                   "reach_rounds": last.reach_rounds,
+                   "phase_ms": {"trim": last.phase_ms[0], "first_pivot": last.phase_ms[1],
+                                "multi_search": last.phase_ms[2], "table_resize": last.phase_ms[3]}},
+        "plain": {"value": plain_rate, "unit": "graphs/s", "sample": len(sample),
+                  "ms_per_graph": plain_ms / len(sample),
+                  "launches_per_graph": plain_launches / len(sample),
+                  "how": f"psc_scc_device on each of {len(sample)} members (every {stride}th), "
+                         "graph resident, CUDA events per call; labels equal to the batch's"},
+        "speedup_vs_plain": value / plain_rate,
+        "e2e": {"value": e2e_value, "unit": "graphs/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s / args.steps * 1e3},
+        "roofline": roofline,
+        "profile": {k: {"launches": v["launches"] // max(1, args.profile_steps),
+                        "ms": v["ms"] / max(1, args.profile_steps)}
+                    for k, v in prof.items() if v["launches"]},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    done, t_total = 0, 0.0
+    for k in sample:
+        mk = g.member(vb, k)
+        t = time.perf_counter()
+        pyoracle.scc(mk.n, mk.off, mk.E, mk.in_off, mk.in_E, seed=int(seeds[k]), nthreads=threads)
+        t_total += time.perf_counter() - t
+        done += 1
+        if t_total > budget_s:
+            break
+    return {"value": done / t_total, "unit": "graphs/s", "cores": threads, "kind": "port",
+            "sample": f"{done} member graphs (every {sample[1] - sample[0] if len(sample) > 1 else 1}"
+                      f"th) solved one by one, {t_total / done * 1e3:.1f} ms each (OpenMP "
+                      "restatement of src/scc.hpp)"}
+
+
+def roofline_of(prof: dict, steps: int) -> dict:
+    fam, top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    peak, peak_kind = peaks()
+    achieved = (top["bytes"] / top["launches"]) / (top["ms"] / top["launches"] / 1e3) / 1e9 \
+        if top["launches"] and top["ms"] > 0 else 0.0
+    prof_total = sum(v["ms"] for v in prof.values())
+    return {
+        "bound": "hbm", "kernel": fam, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+        "launches": top["launches"] // max(1, steps),
+        "share": top["ms"] / prof_total if prof_total else None,
+        "bytes_per_launch": top["bytes"] / max(1, top["launches"]),
+    }
 
 
 def run_gpu(args, world, rank, local, dist) -> None:
@@ -306,18 +551,7 @@ def run_gpu(args, world, rank, local, dist) -> None:
         dg.scc_device(d_labels.value, params)
     prof = dg.profile()
     dg.set_profiling(False)
-    fam, top = max(prof.items(), key=lambda kv: kv[1]["ms"])
-    peak, peak_kind = peaks()
-    achieved = (top["bytes"] / top["launches"]) / (top["ms"] / top["launches"] / 1e3) / 1e9 \
-        if top["launches"] and top["ms"] > 0 else 0.0
-    prof_total = sum(v["ms"] for v in prof.values())
-    roofline = {
-        "bound": "hbm", "kernel": fam, "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-        "launches": top["launches"] // max(1, args.profile_steps),
-        "share": top["ms"] / prof_total if prof_total else None,
-        "bytes_per_launch": top["bytes"] / max(1, top["launches"]),
-    }
+    roofline = roofline_of(prof, args.profile_steps)
 
     # end to end through the C ABI with pinned host buffers
     h2d = h_off.nbytes + h_E.nbytes + h_in_off.nbytes + h_in_E.nbytes
@@ -383,7 +617,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["psc", "reference"], default="psc")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="knn")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="knn")
+    ap.add_argument("--batch-count", type=int, default=4096,
+                    help="graphs in the batch workload")
+    ap.add_argument("--plain-sample", type=int, default=256,
+                    help="batch members solved one by one for the plain comparison")
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-step", action="store_true",
@@ -398,6 +636,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, world, rank, dist)
+        elif args.workload == "batch":
+            run_batch(args, world, rank, local, dist)
         else:
             run_gpu(args, world, rank, local, dist)
     finally:

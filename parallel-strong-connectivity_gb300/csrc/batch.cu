@@ -40,6 +40,9 @@ namespace psc {
 // vertices stay below 2^33, so the bit is free).
 constexpr uint64_t kTrimMark = 1ull << 62;
 
+// Largest frontier of a batch still expanded by VGC rounds.
+constexpr uint64_t kBatchVgcMax = ~0ull;
+
 // ---------------------------------------------------------------------------
 // Graph-offset table
 // ---------------------------------------------------------------------------
@@ -370,7 +373,10 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
     PSC_TRY(ensure_t(g, B_VIS_F, (n + 31) / 32 + 1, &vf));
     PSC_TRY(ensure_t(g, B_VIS_B, (n + 31) / 32 + 1, &vb));
     uint32_t r1 = 0, r2 = 0;
-    PSC_TRY(reach_pair_multi(g, A.srcs, ns, p->local_reach != 0, p->tau, p->pull_div, vf, vb, &r1, &r2));
+    // many small searches at once: VGC for every sparse round, so rounds
+    // shrink by up to tau for the high-diameter members
+    PSC_TRY(reach_pair_multi(g, A.srcs, ns, p->local_reach != 0, p->tau, p->pull_div, vf, vb, &r1,
+                             &r2, kBatchVgcMax));
     g->stats.reach_rounds = r1 + r2;
     {
       ProfScope ps(g, F_LABEL_FIRST);
@@ -444,7 +450,7 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
       }
       MsResult res[2];
       const uint64_t prev[2] = {out_ne, in_ne};
-      PSC_TRY(ms_pair(g, front, nf, 0, labels, p, prev, res, flab));
+      PSC_TRY(ms_pair(g, front, nf, 0, labels, p, prev, res, flab, kBatchVgcMax));
       PSC_TRY(scc_partition(g, res, labels));
       out_ne = res[0].ne;
       in_ne = res[1].ne;
@@ -475,15 +481,14 @@ extern "C" int psc_batch_set(psc_graph_t g, const uint64_t* vbase, uint32_t num_
   for (uint32_t k = 0; k < num_graphs; k++)
     if (vbase[k + 1] < vbase[k]) return PSC_ERR_INVALID;
   PSC_CUDA(cudaSetDevice(g->device));
-  PSC_CUDA(cudaStreamSynchronize(g->stream));
-  if (g->d_vbase) cudaFree(g->d_vbase);
-  if (g->d_gid) cudaFree(g->d_gid);
+  if (g->d_vbase) PSC_CUDA(cudaFreeAsync(g->d_vbase, g->stream));
+  if (g->d_gid) PSC_CUDA(cudaFreeAsync(g->d_gid, g->stream));
   g->d_vbase = nullptr;
   g->d_gid = nullptr;
   g->num_graphs = 0;
   g->vbase.clear();
-  PSC_CUDA(cudaMalloc(&g->d_vbase, ((size_t)num_graphs + 1) * 8));
-  PSC_CUDA(cudaMalloc(&g->d_gid, g->n * 4));
+  PSC_CUDA(cudaMallocAsync((void**)&g->d_vbase, ((size_t)num_graphs + 1) * 8, g->stream));
+  PSC_CUDA(cudaMallocAsync((void**)&g->d_gid, g->n * 4, g->stream));
   PSC_CUDA(cudaMemcpyAsync(g->d_vbase, vbase, ((size_t)num_graphs + 1) * 8, cudaMemcpyHostToDevice,
                            g->stream));
   k_fill_gid<<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(g->d_vbase, num_graphs, g->n, g->d_gid);
@@ -494,8 +499,8 @@ extern "C" int psc_batch_set(psc_graph_t g, const uint64_t* vbase, uint32_t num_
   PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux0, &g->ctr->aux0, 8, cudaMemcpyDeviceToHost, g->stream));
   PSC_CUDA(cudaStreamSynchronize(g->stream));
   if (g->hctr->aux0 != 0) {
-    cudaFree(g->d_vbase);
-    cudaFree(g->d_gid);
+    cudaFreeAsync(g->d_vbase, g->stream);
+    cudaFreeAsync(g->d_gid, g->stream);
     g->d_vbase = nullptr;
     g->d_gid = nullptr;
     return PSC_ERR_INVALID;  // an edge crosses two graphs

@@ -64,7 +64,8 @@ struct Counters {
   unsigned long long unvisited;  // vertices examined by a pull round
   unsigned long long heavy_edges;  // edges scanned by the heavy-vertex kernels
   unsigned long long heavy_probes; // table slots probed by the heavy-pair kernel
-  unsigned long long pad[4];
+  unsigned long long inserted;     // new table entries (multi-search)
+  unsigned long long pad[3];
 };
 constexpr int kCounterSets = 4;
 

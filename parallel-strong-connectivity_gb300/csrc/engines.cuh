@@ -22,24 +22,26 @@ int reach_pair(psc_graph_s* g, uint32_t src, bool local, uint32_t tau, uint32_t 
                uint32_t* vis_f, uint32_t* vis_b, uint32_t* rounds_f, uint32_t* rounds_b);
 
 // Forward and backward reachability from n_srcs device sources at once (the
-// first pivots of a batch of disjoint graphs share one search).
+// first pivots of a batch of disjoint graphs share one search).  vgc_max:
+// largest frontier expanded by VGC rounds (0: one vertex per resident warp).
 int reach_pair_multi(psc_graph_s* g, const uint32_t* d_srcs, uint64_t n_srcs, bool local,
                      uint32_t tau, uint32_t pull_div, uint32_t* vis_f, uint32_t* vis_b,
-                     uint32_t* rounds_f, uint32_t* rounds_b);
+                     uint32_t* rounds_f, uint32_t* rounds_b, uint64_t vgc_max = 0);
 
 // Multi-search (SCC::multi_search, src/scc.hpp:144-275) of one batch in both
 // directions at once: closure of the pivots front[i] (labels label_offset + i)
 // inside their subproblems, left in table slots B_TF (forward) and B_TB
 // (backward).  prev_ne: table sizes of the previous batch (sizing hint).
 // front_labels, when given, holds each pivot's label instead of
-// label_offset + i.
+// label_offset + i.  vgc_max: largest pair frontier expanded by VGC
+// sub-rounds (0: one pair per resident warp).
 struct MsResult {
   uint64_t cap = 0;  // table capacity (power of two)
   uint64_t ne = 0;   // entries
 };
 int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t label_offset,
             const uint64_t* labels, const psc_params_t* p, const uint64_t prev_ne[2],
-            MsResult out[2], const uint32_t* front_labels = nullptr);
+            MsResult out[2], const uint32_t* front_labels = nullptr, uint64_t vgc_max = 0);
 
 // Partition of one batch (src/scc.hpp:437-464): (v, l) in both tables left by
 // ms_pair -> labels[v] = max(l | TOP), else max(l).

@@ -191,18 +191,35 @@ static int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
   return PSC_OK;
 }
 
+// Graph arrays come from the device's stream-ordered pool (kept between
+// handles), so repeated uploads of same-sized graphs do not map new memory.
 static int alloc_graph_arrays(psc_graph_s* g, bool symmetric) {
   const uint64_t n = g->n, m = g->m;
   g->symmetric = symmetric;
-  PSC_CUDA(cudaMalloc(&g->off, (n + 1) * sizeof(uint64_t)));
-  PSC_CUDA(cudaMalloc(&g->E, (m ? m : 1) * sizeof(uint32_t)));
+  PSC_CUDA(cudaMallocAsync((void**)&g->off, (n + 1) * sizeof(uint64_t), g->stream));
+  PSC_CUDA(cudaMallocAsync((void**)&g->E, (m ? m : 1) * sizeof(uint32_t), g->stream));
   if (symmetric) {
     g->in_off = g->off;
     g->in_E = g->E;
   } else {
-    PSC_CUDA(cudaMalloc(&g->in_off, (n + 1) * sizeof(uint64_t)));
-    PSC_CUDA(cudaMalloc(&g->in_E, (m ? m : 1) * sizeof(uint32_t)));
+    PSC_CUDA(cudaMallocAsync((void**)&g->in_off, (n + 1) * sizeof(uint64_t), g->stream));
+    PSC_CUDA(cudaMallocAsync((void**)&g->in_E, (m ? m : 1) * sizeof(uint32_t), g->stream));
   }
+  return PSC_OK;
+}
+
+// Copies the caller's arrays (host or device) into the handle's graph arrays
+// on its stream and waits for them, so the caller may reuse its buffers.
+static int copy_graph_arrays(psc_graph_s* g, const uint64_t* off, const uint32_t* E,
+                             const uint64_t* in_off, const uint32_t* in_E) {
+  const uint64_t n = g->n, m = g->m;
+  PSC_CUDA(cudaMemcpyAsync(g->off, off, (n + 1) * 8, cudaMemcpyDefault, g->stream));
+  if (m) PSC_CUDA(cudaMemcpyAsync(g->E, E, m * 4, cudaMemcpyDefault, g->stream));
+  if (!g->symmetric && in_off) {
+    PSC_CUDA(cudaMemcpyAsync(g->in_off, in_off, (n + 1) * 8, cudaMemcpyDefault, g->stream));
+    if (m) PSC_CUDA(cudaMemcpyAsync(g->in_E, in_E, m * 4, cudaMemcpyDefault, g->stream));
+  }
+  PSC_CUDA(cudaStreamSynchronize(g->stream));
   return PSC_OK;
 }
 
@@ -233,13 +250,7 @@ int psc_graph_upload(const uint64_t* off, const uint32_t* E, const uint64_t* in_
   PSC_TRY(make_handle(n, m, &g));
   bool sym = in_off == nullptr;
   int s = alloc_graph_arrays(g, sym);
-  if (s == PSC_OK) {
-    cudaError_t e = cudaMemcpy(g->off, off, (n + 1) * 8, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && m) e = cudaMemcpy(g->E, E, m * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !sym) e = cudaMemcpy(g->in_off, in_off, (n + 1) * 8, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !sym && m) e = cudaMemcpy(g->in_E, in_E, m * 4, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) s = cuda_status(e);
-  }
+  if (s == PSC_OK) s = copy_graph_arrays(g, off, E, in_off, in_E);
   if (s != PSC_OK) {
     psc_graph_free(g);
     return s;
@@ -256,14 +267,7 @@ int psc_graph_upload_device(const uint64_t* d_off, const uint32_t* d_E, const ui
   PSC_TRY(make_handle(n, m, &g));
   bool sym = d_in_off == nullptr;
   int s = alloc_graph_arrays(g, sym);
-  if (s == PSC_OK) {
-    cudaError_t e = cudaMemcpy(g->off, d_off, (n + 1) * 8, cudaMemcpyDeviceToDevice);
-    if (e == cudaSuccess && m) e = cudaMemcpy(g->E, d_E, m * 4, cudaMemcpyDeviceToDevice);
-    if (e == cudaSuccess && !sym)
-      e = cudaMemcpy(g->in_off, d_in_off, (n + 1) * 8, cudaMemcpyDeviceToDevice);
-    if (e == cudaSuccess && !sym && m) e = cudaMemcpy(g->in_E, d_in_E, m * 4, cudaMemcpyDeviceToDevice);
-    if (e != cudaSuccess) s = cuda_status(e);
-  }
+  if (s == PSC_OK) s = copy_graph_arrays(g, d_off, d_E, d_in_off, d_in_E);
   if (s != PSC_OK) {
     psc_graph_free(g);
     return s;
@@ -279,11 +283,7 @@ int psc_graph_upload_directed(const uint64_t* off, const uint32_t* E, uint64_t n
   psc_graph_s* g = nullptr;
   PSC_TRY(make_handle(n, m, &g));
   int s = alloc_graph_arrays(g, false);
-  if (s == PSC_OK) {
-    cudaError_t e = cudaMemcpy(g->off, off, (n + 1) * 8, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && m) e = cudaMemcpy(g->E, E, m * 4, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) s = cuda_status(e);
-  }
+  if (s == PSC_OK) s = copy_graph_arrays(g, off, E, nullptr, nullptr);
   if (s == PSC_OK) s = build_transpose(g);
   if (s == PSC_OK) {
     cudaError_t e = cudaStreamSynchronize(g->stream);
@@ -312,15 +312,15 @@ int psc_graph_free(psc_graph_t g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   for (auto& b : g->bufs)
     if (b.p) cudaFreeAsync(b.p, g->stream);
+  if (g->in_off && g->in_off != g->off) cudaFreeAsync(g->in_off, g->stream);
+  if (g->in_E && g->in_E != g->E) cudaFreeAsync(g->in_E, g->stream);
+  if (g->off) cudaFreeAsync(g->off, g->stream);
+  if (g->E) cudaFreeAsync(g->E, g->stream);
+  if (g->d_vbase) cudaFreeAsync(g->d_vbase, g->stream);
+  if (g->d_gid) cudaFreeAsync(g->d_gid, g->stream);
   if (g->stream) cudaStreamSynchronize(g->stream);
-  if (g->in_off && g->in_off != g->off) cudaFree(g->in_off);
-  if (g->in_E && g->in_E != g->E) cudaFree(g->in_E);
-  if (g->off) cudaFree(g->off);
-  if (g->E) cudaFree(g->E);
   if (g->ctr) cudaFree(g->ctr);
   if (g->hctr) cudaFreeHost(g->hctr);
-  if (g->d_vbase) cudaFree(g->d_vbase);
-  if (g->d_gid) cudaFree(g->d_gid);
   for (auto& p : g->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);

@@ -53,6 +53,7 @@ struct MsSide {
   uint64_t* Fheavy;
   uint32_t* hflag;
   Counters* ctr;
+  uint32_t vgc_budget;  // new pairs one VGC local search may insert
 };
 
 // Per-warp source data of one expansion step.
@@ -215,7 +216,14 @@ __device__ __forceinline__ void flush_ms_counters(Counters* c0, Counters* c1,
                                                   unsigned long long s0, unsigned long long s1,
                                                   unsigned long long r0, unsigned long long r1,
                                                   unsigned long long p0, unsigned long long p1,
-                                                  unsigned long long x0, unsigned long long x1) {
+                                                  unsigned long long x0, unsigned long long x1,
+                                                  unsigned long long i0, unsigned long long i1) {
+  i0 = warp_sum(i0);
+  i1 = warp_sum(i1);
+  if (lane_id() == 0) {
+    if (i0) atomicAdd(&c0->inserted, i0);
+    if (i1) atomicAdd(&c1->inserted, i1);
+  }
   s0 = warp_sum(s0);
   s1 = warp_sum(s1);
   r0 = warp_sum(r0);
@@ -257,7 +265,7 @@ __global__ void __launch_bounds__(BLOCK, 3)
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint64_t c0 = (s0.nin + 31) / 32, c1 = (s1.nin + 31) / 32;
   MsSrc& src = ssrc[wid];
-  unsigned long long sc0 = 0, sc1 = 0, rq0 = 0, rq1 = 0, ex0 = 0, ex1 = 0;
+  unsigned long long sc0 = 0, sc1 = 0, rq0 = 0, rq1 = 0, ex0 = 0, ex1 = 0, in0 = 0, in1 = 0;
   uint32_t pr0 = 0, pr1 = 0;
   for (uint64_t c = gw; c < c0 + c1; c += nw) {
     const int sd = c < c0 ? 0 : 1;
@@ -289,6 +297,7 @@ __global__ void __launch_bounds__(BLOCK, 3)
     ms_expand_claim<kMsExpandK, false, false>(
         sm[wid], src, beg, deg, S.off, S.E, labels, S.T, S.mask, probes,
         [&](uint32_t tm, const uint64_t* keys) {
+          (sd ? in1 : in0) += __popc(tm);
           warp_append_batch<kMsExpandK>(tm, keys, S.Fout, &S.ctr->next);
         });
     (sd ? pr1 : pr0) += probes;
@@ -301,7 +310,7 @@ __global__ void __launch_bounds__(BLOCK, 3)
     }
     __syncwarp();
   }
-  flush_ms_counters(s0.ctr, s1.ctr, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1);
+  flush_ms_counters(s0.ctr, s1.ctr, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1, in0, in1);
 }
 
 struct MsQEnt {
@@ -314,7 +323,7 @@ struct MsQEnt {
 // label and adjacency range are loaded together, then the first table probes
 // (atomicCAS) of all K candidates are issued before any is resolved.  Returns
 // the mask of new pairs; sets *failed if an insert gave up.
-template <int K>
+template <int K, bool ADJ = true>
 __device__ __forceinline__ uint32_t ms_vgc_claim(const uint32_t* w, uint64_t* vb, uint64_t* ve,
                                                  uint64_t sub, uint32_t lab,
                                                  const uint64_t* __restrict__ off,
@@ -328,8 +337,10 @@ __device__ __forceinline__ uint32_t ms_vgc_claim(const uint32_t* w, uint64_t* vb
     vb[k] = ve[k] = 0;
     if (w[k] != 0xFFFFFFFFu) {
       const uint64_t lw = __ldg(&labels[w[k]]);
-      vb[k] = __ldg(&off[w[k]]);
-      ve[k] = __ldg(&off[w[k] + 1]);
+      if (ADJ) {
+        vb[k] = __ldg(&off[w[k]]);
+        ve[k] = __ldg(&off[w[k] + 1]);
+      }
       if (lw == sub) key[k] = ((uint64_t)w[k] << 32) | lab;
     }
   }
@@ -412,7 +423,7 @@ __global__ void __launch_bounds__(BLOCK)
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
   MsQEnt* Q = sq[wid];
-  unsigned long long sc0 = 0, sc1 = 0, rq0 = 0, rq1 = 0, ex0 = 0, ex1 = 0;
+  unsigned long long sc0 = 0, sc1 = 0, rq0 = 0, rq1 = 0, ex0 = 0, ex1 = 0, in0 = 0, in1 = 0;
   uint32_t pr0 = 0, pr1 = 0;
   if (lane == 0) sm[wid].fail = 0;
   __syncwarp();
@@ -440,21 +451,26 @@ __global__ void __launch_bounds__(BLOCK)
         }
         continue;
       }
+      // a vertex with tau..kHeavyDeg out-edges: the warp walks them with
+      // kMsK edges per lane in flight
       if (lane == 0) (sd ? sc1 : sc0) += du;
       bool failed = false;
-      for (uint64_t b = ub; b < ue; b += 32) {
-        const uint64_t e = b + lane;
-        bool take = false;
-        uint32_t w = 0;
-        if (e < ue) {
-          w = __ldg(&S.E[e]);
-          if (__ldg(&labels[w]) == sub) {
-            int r = table_insert(S.T, S.mask, ((uint64_t)w << 32) | lab, kProbeLimit, &probes);
-            take = r == 1;
-            failed |= r < 0;
-          }
+      for (uint64_t b = ub; b < ue; b += 32 * kMsK) {
+        uint32_t w[kMsK];
+        uint64_t vb[kMsK], ve[kMsK], keys[kMsK];
+#pragma unroll
+        for (int k = 0; k < kMsK; k++) {
+          const uint64_t e = b + k * 32 + lane;
+          w[k] = e < ue ? __ldg(&S.E[e]) : 0xFFFFFFFFu;
         }
-        emit(take, w);
+        bool fk = false;
+        const uint32_t tm = ms_vgc_claim<kMsK, false>(w, vb, ve, sub, lab, S.off, labels, S.T,
+                                                      S.mask, probes, fk);
+        failed |= fk;
+        (sd ? in1 : in0) += __popc(tm);
+#pragma unroll
+        for (int k = 0; k < kMsK; k++) keys[k] = ((uint64_t)w[k] << 32) | lab;
+        warp_append_batch<kMsK>(tm, keys, S.Fout, &S.ctr->next);
       }
       (sd ? pr1 : pr0) += probes;
       const bool rq = __any_sync(kFull, failed) && lane == 0;
@@ -464,8 +480,10 @@ __global__ void __launch_bounds__(BLOCK)
     }
     if (lane == 0) Q[0] = MsQEnt{ub, u, (uint32_t)du};
     __syncwarp();
-    uint32_t head = 0, tail = 1;
-    while (head < tail && tail < tq) {
+    // the local search stops at tq queued vertices, or once it has inserted
+    // its share of the table's free room (the first wave always runs)
+    uint32_t head = 0, tail = 1, ins = 0;
+    while (head < tail && tail < tq && (head == 0 || ins < S.vgc_budget)) {
       const uint32_t wave = min(32u, tail - head);
       uint64_t beg = 0;
       uint32_t deg = 0, x = 0;
@@ -527,6 +545,8 @@ __global__ void __launch_bounds__(BLOCK)
           for (int k = 0; k < kMsK; k++)
             if (w[k] != 0xFFFFFFFFu) atomicOr(&sm[wid].fail, 1u << sl[k]);
         }
+        (sd ? in1 : in0) += __popc(tm);
+        ins += __reduce_add_sync(kFull, (unsigned)__popc(tm));
         ms_vgc_place<kMsK>(tm, w, vb, ve, lab, Q, tail, tq, S.Fout, &S.ctr->next);
       }
       __syncwarp();
@@ -553,7 +573,7 @@ __global__ void __launch_bounds__(BLOCK)
     }
     __syncwarp();
   }
-  flush_ms_counters(s0.ctr, s1.ctr, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1);
+  flush_ms_counters(s0.ctr, s1.ctr, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1, in0, in1);
 }
 
 // Heavy pairs of both sides: the whole grid walks each one's edges.
@@ -567,7 +587,7 @@ __global__ void __launch_bounds__(BLOCK)
     const MsSide S = sd ? s1 : s0;
     if (!S.ctr) continue;
     const uint64_t nh = *(volatile unsigned long long*)&S.ctr->heavy;
-    unsigned long long scanned = 0, requeued = 0;
+    unsigned long long scanned = 0, requeued = 0, ins = 0;
     uint32_t probes = 0;
     for (uint64_t hh = 0; hh < nh; hh++) {
       const uint64_t key = S.Fheavy[hh];
@@ -590,6 +610,7 @@ __global__ void __launch_bounds__(BLOCK)
             failed |= r < 0;
           }
         }
+        ins += take ? 1 : 0;
         unsigned long long pos = warp_append(&S.ctr->next, take);
         if (take) S.Fout[pos] = nk;
       }
@@ -604,8 +625,10 @@ __global__ void __launch_bounds__(BLOCK)
     }
     scanned = warp_sum(scanned);
     requeued = warp_sum(requeued);
+    ins = warp_sum(ins);
     unsigned long long pr = warp_sum((unsigned long long)probes);
     if (lane == 0) {
+      if (ins) atomicAdd(&S.ctr->inserted, ins);
       if (scanned) atomicAdd(&S.ctr->heavy_edges, scanned);
       if (pr) atomicAdd(&S.ctr->heavy_probes, pr);
       if (requeued) {
@@ -664,6 +687,11 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
   r.Fheavy = (uint64_t*)g->bufs[s.h_slot].p;
   r.hflag = (uint32_t*)g->bufs[s.f_slot].p;
   r.ctr = g->ctr + s.cset;
+  // VGC local searches share the room left below half load, so one
+  // sub-round cannot fill the table
+  const uint64_t room = s.cap / 2 > s.ne ? s.cap / 2 - s.ne : 0;
+  const uint64_t share = room / (s.nf ? s.nf : 1);
+  r.vgc_budget = (uint32_t)(share < 0xFFFFFFFFull ? share : 0xFFFFFFFFull);
   return r;
 }
 
@@ -671,16 +699,18 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
 
 int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t label_offset,
             const uint64_t* labels, const psc_params_t* p, const uint64_t prev_ne[2],
-            MsResult out[2], const uint32_t* front_labels) {
+            MsResult out[2], const uint32_t* front_labels, uint64_t vgc_max) {
   const uint32_t tau = p->tau ? p->tau : 512;
   const bool local = p->local_scc != 0;
-  const uint64_t vgc_limit = (uint64_t)g->num_sms * 32;
+  const uint64_t vgc_limit = vgc_max ? vgc_max : (uint64_t)g->num_sms * 32;
   MsState st[2];
   st[0] = MsState{false, B_TF, B_PA, B_PB, B_PH, B_AUX1, 0};
   st[1] = MsState{true, B_TB, B_PA2, B_PB2, B_PH2, B_HF2, 1};
   for (int k = 0; k < 2; k++) {
     MsState& s = st[k];
-    s.cap = pow2_at_least(std::max<uint64_t>({4096, 4 * n_front, 2 * prev_ne[k]}));
+    const uint64_t want0 = (local && n_front <= vgc_limit) ? n_front * std::min<uint32_t>(tau, 64) : 0;
+    s.cap = pow2_at_least(std::max<uint64_t>(
+        {4096, 4 * n_front, 2 * prev_ne[k], std::min<uint64_t>(1ull << 27, 2 * (n_front + want0))}));
     void* q;
     PSC_TRY(ensure(g, s.t_slot, s.cap * 8 + 16, &q));
     PSC_CUDA(cudaMemsetAsync(q, 0xFF, s.cap * 8, g->stream));
@@ -704,9 +734,15 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       if (s.nf == 0) continue;
       any = true;
       g->stats.subrounds++;
-      if (s.grow || 2 * s.ne > s.cap) {
+      // room for the VGC local searches of this sub-round: up to
+      // min(tq, 64) new pairs each, while the table stays below 2^27 slots
+      const uint64_t want = (local && s.nf <= vgc_limit) ? s.nf * std::min<uint32_t>(tau, 64) : 0;
+      const bool vgc_room = want && s.cap < (1ull << 27) && s.ne + want > s.cap / 2;
+      if (s.grow || 2 * s.ne > s.cap || vgc_room) {
         // keep the load at most 1/2 (1/4 right after growing)
         uint64_t cap2 = pow2_at_least(std::max<uint64_t>(4 * s.ne, 2 * s.cap));
+        if (vgc_room)
+          cap2 = std::max(cap2, std::min<uint64_t>(1ull << 27, pow2_at_least(2 * (s.ne + want))));
         if (cap2 > (1ull << 40)) return PSC_ERR_TABLE_FULL;
         PSC_TRY(ms_grow(g, s.t_slot, s.cap, cap2));
         s.cap = cap2;
@@ -766,13 +802,20 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
           }
     }
     if (trace_on()) {
+      cudaEvent_t tr = take_event(g);
+      PSC_CUDA(cudaEventRecord(tr, g->stream));
+      PSC_CUDA(cudaEventSynchronize(tr));
+      float ms = 0;  // since the start of the call
+      cudaEventElapsedTime(&ms, g->t0, tr);
+      give_event(g, tr);
       for (int k = 0; k < 2; k++)
         if (st[k].nf)
-          std::fprintf(stderr, "ms side %d mode %s nf %llu next %llu edges %llu probes %llu cap %llu ne %llu\n",
+          std::fprintf(stderr, "ms side %d mode %s nf %llu next %llu edges %llu probes %llu "
+                       "expanded %llu cap %llu ne %llu t %.3f ms\n",
                        k, is_vgc[k] ? "vgc" : "expand", (unsigned long long)st[k].nf,
                        g->hctr[st[k].cset].next, g->hctr[st[k].cset].edges,
-                       g->hctr[st[k].cset].probes, (unsigned long long)st[k].cap,
-                       (unsigned long long)st[k].ne);
+                       g->hctr[st[k].cset].probes, g->hctr[st[k].cset].expanded,
+                       (unsigned long long)st[k].cap, (unsigned long long)st[k].ne, ms);
     }
     for (int k = 0; k < 2; k++) {
       MsState& s = st[k];
@@ -784,7 +827,7 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
         g->prof[is_vgc[k] ? F_MS_VGC : F_MS_EXPAND].bytes +=
             8.0 * s.nf + 16.0 * c.expanded + 12.0 * c.edges + 8.0 * c.probes + 8.0 * c.next;
       }
-      s.ne += c.next - c.aux1;
+      s.ne += c.inserted;
       s.grow = c.fail > 0;
       std::swap(g->bufs[s.a_slot], g->bufs[s.b_slot]);
       s.nf = c.next;

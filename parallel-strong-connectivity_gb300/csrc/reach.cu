@@ -286,20 +286,24 @@ __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1,
         if (lane == 0) S.heavy[atomicAdd(&S.ctr->heavy, 1ull)] = u;
         continue;
       }
+      // a vertex with tau..kHeavyDeg out-edges: the warp walks them with
+      // kExpandK edges per lane in flight
       if (lane == 0) (sd ? scanned1 : scanned0) += du;
-      for (uint64_t b = ub; b < ue; b += 32) {
-        const uint64_t e = b + lane;
-        uint32_t v = 0;
-        bool take = false;
-        if (e < ue) {
-          v = __ldg(&S.E[e]);
-          take = bit_set(S.vis, v);
+      for (uint64_t b = ub; b < ue; b += 32 * kExpandK) {
+        uint32_t v[kExpandK];
+#pragma unroll
+        for (int k = 0; k < kExpandK; k++) {
+          const uint64_t e = b + k * 32 + lane;
+          v[k] = e < ue ? __ldg(&S.E[e]) : 0xFFFFFFFFu;
         }
-        unsigned long long pos = warp_append(&S.ctr->next, take);
-        if (take) {
-          S.qout[pos] = v;
-          nedges += S.off[v + 1] - S.off[v];
-        }
+        uint32_t tm = 0;
+#pragma unroll
+        for (int k = 0; k < kExpandK; k++)
+          if (v[k] != 0xFFFFFFFFu && bit_set(S.vis, v[k])) tm |= 1u << k;
+#pragma unroll
+        for (int k = 0; k < kExpandK; k++)
+          if (tm & (1u << k)) nedges += S.off[v[k] + 1] - S.off[v[k]];
+        warp_append_batch<kExpandK>(tm, v, S.qout, &S.ctr->next);
       }
       continue;
     }
@@ -557,10 +561,11 @@ Side make_side(bool backward, uint32_t* vis, int second) {
 // sources d_srcs.
 static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs, bool local,
                        uint32_t tau, uint32_t pull_div, const uint32_t* d_srcs = nullptr,
-                       uint64_t n_dsrc = 0) {
+                       uint64_t n_dsrc = 0, uint64_t vgc_max = 0) {
   const uint64_t n = g->n, nwords = (n + 31) / 32;
   // VGC rounds while the frontier is below one vertex per resident warp
-  const uint64_t vgc_limit = (uint64_t)g->num_sms * 64;
+  // (unless the caller sets the limit)
+  const uint64_t vgc_limit = vgc_max ? vgc_max : (uint64_t)g->num_sms * 64;
   if (pull_div == 0) pull_div = 20;
   const uint64_t threshold = g->m / pull_div;
   for (int k = 0; k < ns; k++) {
@@ -726,9 +731,9 @@ int reach_pair(psc_graph_s* g, uint32_t src, bool local, uint32_t tau, uint32_t 
 
 int reach_pair_multi(psc_graph_s* g, const uint32_t* d_srcs, uint64_t n_srcs, bool local,
                      uint32_t tau, uint32_t pull_div, uint32_t* vis_f, uint32_t* vis_b,
-                     uint32_t* rounds_f, uint32_t* rounds_b) {
+                     uint32_t* rounds_f, uint32_t* rounds_b, uint64_t vgc_max) {
   Side s[2] = {make_side(false, vis_f, 0), make_side(true, vis_b, 1)};
-  PSC_TRY(reach_sides(g, s, 2, nullptr, local, tau ? tau : 512, pull_div, d_srcs, n_srcs));
+  PSC_TRY(reach_sides(g, s, 2, nullptr, local, tau ? tau : 512, pull_div, d_srcs, n_srcs, vgc_max));
   if (rounds_f) *rounds_f = s[0].rounds;
   if (rounds_b) *rounds_b = s[1].rounds;
   return PSC_OK;

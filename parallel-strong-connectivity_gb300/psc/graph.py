@@ -157,6 +157,22 @@ class HostGraph:
             u.in_off, u.in_E = cat("in_off", "in_E")
         return u, vb
 
+    def member(self, vbase: np.ndarray, k: int) -> "HostGraph":
+        """Graph k of a packed batch, with local vertex ids."""
+        v0, v1 = int(vbase[k]), int(vbase[k + 1])
+        e0, e1 = int(self.off[v0]), int(self.off[v1])
+        off = (self.off[v0:v1 + 1] - e0).astype(np.uint64)
+        E = (self.E[e0:e1].astype(np.int64) - v0).astype(np.uint32)
+        g = HostGraph(v1 - v0, e1 - e0, off, E)
+        if self.symmetric:
+            g.symmetric = True
+            g.in_off, g.in_E = g.off, g.E
+        elif self.in_off is not None:
+            f0, f1 = int(self.in_off[v0]), int(self.in_off[v1])
+            g.in_off = (self.in_off[v0:v1 + 1] - f0).astype(np.uint64)
+            g.in_E = (self.in_E[f0:f1].astype(np.int64) - v0).astype(np.uint32)
+        return g
+
     def edge_list(self) -> tuple[np.ndarray, np.ndarray]:
         src = np.repeat(np.arange(self.n, dtype=np.uint32), np.diff(self.off).astype(np.int64))
         return src, self.E

@@ -19,22 +19,7 @@ def _dev(cuda_device):
 
 def members_of(u, vbase):
     """Split a packed union back into its member graphs (local ids)."""
-    out = []
-    for k in range(len(vbase) - 1):
-        v0, v1 = int(vbase[k]), int(vbase[k + 1])
-        e0, e1 = int(u.off[v0]), int(u.off[v1])
-        off = (u.off[v0:v1 + 1] - e0).astype(np.uint64)
-        E = (u.E[e0:e1].astype(np.int64) - v0).astype(np.uint32)
-        g = psc.HostGraph(v1 - v0, e1 - e0, off, E)
-        if u.symmetric:
-            g.symmetric = True
-            g.in_off, g.in_E = g.off, g.E
-        else:
-            f0 = int(u.in_off[v0])
-            g.in_off = (u.in_off[v0:v1 + 1] - f0).astype(np.uint64)
-            g.in_E = (u.in_E[f0:int(u.in_off[v1])].astype(np.int64) - v0).astype(np.uint32)
-        out.append(g)
-    return out
+    return [u.member(vbase, k) for k in range(len(vbase) - 1)]
 
 
 def check_scc_batch(graphs, params, seeds=None, plain=False):

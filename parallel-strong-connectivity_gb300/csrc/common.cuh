@@ -65,7 +65,8 @@ struct Counters {
   unsigned long long heavy_edges;  // edges scanned by the heavy-vertex kernels
   unsigned long long heavy_probes; // table slots probed by the heavy-pair kernel
   unsigned long long inserted;     // new table entries (multi-search)
-  unsigned long long pad[3];
+  unsigned long long waves;        // local-search waves of VGC rounds (trace)
+  unsigned long long pad[2];
 };
 constexpr int kCounterSets = 4;
 
@@ -101,6 +102,8 @@ struct psc_graph_s {
   uint64_t* in_off = nullptr;  // aliases off for symmetric graphs
   uint32_t* in_E = nullptr;
   int num_sms = 0;
+  int vgc_blocks = 0;     // resident blocks per SM of the reach VGC kernel
+  int ms_vgc_blocks = 0;  // same for the multi-search VGC kernel
   // named scratch buffers, grown on demand (stream-ordered allocator)
   std::vector<psc::DevBuf> bufs;
   psc::Counters* ctr = nullptr;   // device, kCounterSets blocks

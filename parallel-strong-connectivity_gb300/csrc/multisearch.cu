@@ -774,9 +774,17 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
     }
     if (nv) {
       ProfScope ps(g, F_MS_VGC);
-      k_ms_vgc<kMsVgcBlock, kMsVgcQueue>
-          <<<grid_for(g, v_items * 32, kMsVgcBlock), kMsVgcBlock, 0, g->stream>>>(vg[0], vg[1], labels,
-                                                                                   tau);
+      // a resident grid, one pair per warp at a time
+      if (!g->ms_vgc_blocks) {
+        PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &g->ms_vgc_blocks, k_ms_vgc<kMsVgcBlock, kMsVgcQueue>, kMsVgcBlock, 0));
+        if (g->ms_vgc_blocks < 1) g->ms_vgc_blocks = 1;
+      }
+      const uint64_t max_blocks = (uint64_t)g->num_sms * g->ms_vgc_blocks;
+      const uint64_t blocks =
+          std::min(max_blocks, (v_items + kMsVgcBlock / 32 - 1) / (kMsVgcBlock / 32));
+      k_ms_vgc<kMsVgcBlock, kMsVgcQueue><<<(unsigned)std::max<uint64_t>(1, blocks), kMsVgcBlock, 0,
+                                           g->stream>>>(vg[0], vg[1], labels, tau);
     }
     if (ne) {
       ProfScope ps(g, F_MS_EXPAND);

@@ -208,7 +208,7 @@ __device__ __forceinline__ void vgc_place(uint32_t tm, const uint32_t* w, const 
   }
   const uint32_t total = __shfl_sync(kFull, incl, 31);
   if (total == 0) return;
-  const uint32_t room = tq - tail;
+  const uint32_t room = tail < tq ? tq - tail : 0;
   const uint32_t nloc = total < room ? total : room;
   unsigned long long sbase = 0;
   if (total > nloc && lane == 0) sbase = atomicAdd(next_ctr, (unsigned long long)(total - nloc));
@@ -254,63 +254,86 @@ __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, u
   return tm;
 }
 
-// VGC round for up to two sides: one frontier vertex per warp.  A vertex with
-// 0 < deg < tau starts a local BFS in a shared-memory queue of tq =
+// A frontier vertex with tau..kHeavyDeg out-edges: the warp walks them with
+// kExpandK edges per lane in flight.
+__device__ __forceinline__ void vgc_direct(const ReachSide& S, uint64_t ub, uint64_t du,
+                                           unsigned long long& nedges) {
+  const unsigned lane = lane_id();
+  const uint64_t ue = ub + du;
+  for (uint64_t b = ub; b < ue; b += 32 * kExpandK) {
+    uint32_t v[kExpandK];
+#pragma unroll
+    for (int k = 0; k < kExpandK; k++) {
+      const uint64_t e = b + k * 32 + lane;
+      v[k] = e < ue ? __ldg(&S.E[e]) : 0xFFFFFFFFu;
+    }
+    uint32_t tm = 0;
+#pragma unroll
+    for (int k = 0; k < kExpandK; k++)
+      if (v[k] != 0xFFFFFFFFu && bit_set(S.vis, v[k])) tm |= 1u << k;
+#pragma unroll
+    for (int k = 0; k < kExpandK; k++)
+      if (tm & (1u << k)) nedges += S.off[v[k] + 1] - S.off[v[k]];
+    warp_append_batch<kExpandK>(tm, v, S.qout, &S.ctr->next);
+  }
+}
+
+// VGC round for up to two sides.  Each warp takes a chunk of up to `chunk`
+// frontier vertices (one when the frontier is small, up to 32 when it is much
+// larger than the grid, so every warp has work).  Chunk vertices with
+// 0 < deg < tau seed a local BFS in a shared-memory queue of tq =
 // min(tau, QCAP) entries: each wave takes up to 32 queued vertices and claims
-// their neighbours on the bitmap (one vertex per lane when all their degrees
-// are at most K, else the balanced expansion), keeping claimed vertices in the
-// queue while it has room and spilling the rest to the next frontier.  Queued
-// vertices with more than tq out-edges, and whatever is left in the queue when
-// it fills, are spilled too.  Other frontier vertices are expanded directly
-// (heavy ones by the whole grid).
+// their neighbours on the bitmap (balanced expansion, K edges per lane in
+// flight), keeping claimed vertices in the queue while it has room and
+// spilling the rest to the next frontier.  Queued vertices with more than tq
+// out-edges, and whatever is left in the queue when it fills, are spilled too.
+// Other chunk vertices are expanded directly (heavy ones by the whole grid).
 template <int BLOCK, int QCAP>
-__global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau) {
+__global__ void __launch_bounds__(BLOCK)
+    k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau, uint32_t chunk) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ QEnt sq[BLOCK / 32][QCAP];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
+  uint32_t C = chunk < tq ? chunk : tq;
+  C = C < 1 ? 1 : C > 32 ? 32 : C;
   QEnt* Q = sq[wid];
   unsigned long long scanned0 = 0, scanned1 = 0, nedges0 = 0, nedges1 = 0, exp0 = 0, exp1 = 0;
-  for (uint64_t i = gw; i < s0.nin + s1.nin; i += nw) {
-    const int sd = i < s0.nin ? 0 : 1;
+  unsigned long long wv0 = 0, wv1 = 0;  // waves (warp-uniform)
+  const uint64_t c0 = (s0.nin + C - 1) / C, c1 = (s1.nin + C - 1) / C;
+  for (uint64_t c = gw; c < c0 + c1; c += nw) {
+    const int sd = c < c0 ? 0 : 1;
     const ReachSide S = sd ? s1 : s0;
     unsigned long long& nedges = sd ? nedges1 : nedges0;
-    const uint32_t u = S.qin[sd ? i - s0.nin : i];
-    const uint64_t ub = S.off[u], ue = S.off[u + 1];
-    const uint64_t du = ue - ub;
-    if (lane == 0) (sd ? exp1 : exp0)++;
-    if (!(du > 0 && du < tq)) {
-      if (du > kHeavyDeg) {
-        if (lane == 0) S.heavy[atomicAdd(&S.ctr->heavy, 1ull)] = u;
-        continue;
-      }
-      // a vertex with tau..kHeavyDeg out-edges: the warp walks them with
-      // kExpandK edges per lane in flight
-      if (lane == 0) (sd ? scanned1 : scanned0) += du;
-      for (uint64_t b = ub; b < ue; b += 32 * kExpandK) {
-        uint32_t v[kExpandK];
-#pragma unroll
-        for (int k = 0; k < kExpandK; k++) {
-          const uint64_t e = b + k * 32 + lane;
-          v[k] = e < ue ? __ldg(&S.E[e]) : 0xFFFFFFFFu;
-        }
-        uint32_t tm = 0;
-#pragma unroll
-        for (int k = 0; k < kExpandK; k++)
-          if (v[k] != 0xFFFFFFFFu && bit_set(S.vis, v[k])) tm |= 1u << k;
-#pragma unroll
-        for (int k = 0; k < kExpandK; k++)
-          if (tm & (1u << k)) nedges += S.off[v[k] + 1] - S.off[v[k]];
-        warp_append_batch<kExpandK>(tm, v, S.qout, &S.ctr->next);
-      }
-      continue;
+    const uint64_t first = (sd ? c - c0 : c) * C;
+    const uint64_t left = S.nin - first;
+    const uint32_t cnt = left < C ? (uint32_t)left : C;
+    uint32_t u = 0;
+    uint64_t ub = 0, du = 0;
+    if (lane < cnt) {
+      u = S.qin[first + lane];
+      ub = S.off[u];
+      du = S.off[u + 1] - ub;
+      (sd ? exp1 : exp0)++;
+      if (du > kHeavyDeg) S.heavy[atomicAdd(&S.ctr->heavy, 1ull)] = u;
     }
-    if (lane == 0) Q[0] = QEnt{ub, u, (uint32_t)du};
+    uint32_t big = __ballot_sync(kFull, lane < cnt && du >= tq && du <= kHeavyDeg);
+    while (big) {
+      const int l = __ffs(big) - 1;
+      big &= big - 1;
+      const uint64_t bb = __shfl_sync(kFull, ub, l), bd = __shfl_sync(kFull, du, l);
+      if (lane == 0) (sd ? scanned1 : scanned0) += bd;
+      vgc_direct(S, bb, bd, nedges);
+    }
+    const bool seed = lane < cnt && du > 0 && du < tq;
+    const uint32_t smask = __ballot_sync(kFull, seed);
+    if (seed) Q[__popc(smask & ((1u << lane) - 1))] = QEnt{ub, u, (uint32_t)du};
+    const uint32_t nseed = __popc(smask);
     __syncwarp();
-    uint32_t head = 0, tail = 1;
-    while (head < tail && tail < tq) {
+    uint32_t head = 0, tail = nseed;
+    while (head < tail && (head == 0 || tail < tq)) {
       const uint32_t wave = min(32u, tail - head);
       uint64_t beg = 0;
       uint32_t deg = 0, x = 0, xdeg = 0;
@@ -325,9 +348,10 @@ __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1,
           spill_self = true;
           deg = 0;
         }
-        if (lane > 0 || head > 0) (sd ? exp1 : exp0)++;
+        if (head + lane >= nseed) (sd ? exp1 : exp0)++;
       }
       head += wave;
+      (sd ? wv1 : wv0)++;
       __syncwarp();
       if (__any_sync(kFull, spill_self)) {
         unsigned long long pos = warp_append(&S.ctr->next, spill_self);
@@ -378,6 +402,10 @@ __global__ void __launch_bounds__(BLOCK) k_reach_vgc(ReachSide s0, ReachSide s1,
     }
     __syncwarp();
   }
+  if (lane == 0) {
+    if (wv0) atomicAdd(&s0.ctr->waves, wv0);
+    if (wv1) atomicAdd(&s1.ctr->waves, wv1);
+  }
   flush_side_counters(s0.ctr, s1.ctr, scanned0, scanned1, nedges0, nedges1, exp0, exp1);
 }
 
@@ -422,7 +450,18 @@ __global__ void __launch_bounds__(BLOCK) k_reach_heavy(ReachSide s0, ReachSide s
 }
 
 // Pull round: B_* is the reverse direction of the search, A_off the search
-// direction's offsets (for the next round's edge count).
+// direction's offsets (for the next round's edge count).  A warp owns 32
+// consecutive vertices; each unvisited one scans its in-edges for a frontier
+// vertex, kPullP edges in flight, alone for its first kPullSolo in-edges; the
+// longer in-lists left over are then scanned by the whole warp, one vertex at
+// a time, 32 * kPullP edges per step, until a hit.
+constexpr int kPullP = 4;
+constexpr uint32_t kPullSolo = 64;
+
+__device__ __forceinline__ bool fb_test(const uint32_t* __restrict__ fb, uint32_t x) {
+  return (__ldg(&fb[x >> 5]) >> (x & 31)) & 1u;
+}
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
@@ -436,21 +475,59 @@ __global__ void __launch_bounds__(BLOCK)
   for (uint64_t w = gw; w < nwords; w += nw) {
     const uint64_t v = w * 32 + lane;
     const uint32_t vw = vis[w];
+    const bool todo = v < n && !((vw >> lane) & 1u);
     bool found = false;
-    if (v < n && !((vw >> lane) & 1u)) {
+    uint64_t j = 0, e = 0;
+    if (todo) {
       unvisited++;
-      const uint64_t b = B_off[v], e = B_off[v + 1];
-      uint64_t j = b;
-      for (; j < e; j++) {
-        uint32_t x = __ldg(&B_E[j]);
-        if ((__ldg(&fb_in[x >> 5]) >> (x & 31)) & 1u) {
-          found = true;
-          break;
-        }
+      const uint64_t b = B_off[v];
+      e = B_off[v + 1];
+      j = b;
+      const uint64_t lim = e < b + kPullSolo ? e : b + kPullSolo;
+      // the first in-edge alone (dense rounds often hit at once), then
+      // kPullP at a time
+      if (j < lim) {
+        found = fb_test(fb_in, __ldg(&B_E[j]));
+        j++;
       }
-      scanned += (found ? j + 1 : j) - b;
-      if (found) next_edges += A_off[v + 1] - A_off[v];
+      while (j < lim && !found) {
+        uint32_t x[kPullP];
+#pragma unroll
+        for (int k = 0; k < kPullP; k++) x[k] = j + k < lim ? __ldg(&B_E[j + k]) : 0xFFFFFFFFu;
+        bool hit[kPullP];
+#pragma unroll
+        for (int k = 0; k < kPullP; k++) hit[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
+        uint64_t step = lim - j < (uint64_t)kPullP ? lim - j : (uint64_t)kPullP;
+#pragma unroll
+        for (int k = kPullP - 1; k >= 0; k--)
+          if (hit[k]) {
+            found = true;
+            step = k + 1;
+          }
+        j += step;
+      }
+      scanned += j - b;
     }
+    uint32_t longm = __ballot_sync(kFull, todo && !found && j < e);
+    while (longm) {
+      const int l = __ffs(longm) - 1;
+      longm &= longm - 1;
+      const uint64_t lb = __shfl_sync(kFull, j, l), le = __shfl_sync(kFull, e, l);
+      bool f = false;
+      uint64_t jj = lb;
+      for (; jj < le && !f; jj += 32 * kPullP) {
+        bool hit = false;
+#pragma unroll
+        for (int k = 0; k < kPullP; k++) {
+          const uint64_t q = jj + k * 32 + lane;
+          if (q < le) hit |= fb_test(fb_in, __ldg(&B_E[q]));
+        }
+        f = __any_sync(kFull, hit);
+      }
+      if (lane == 0) scanned += (jj < le ? jj : le) - lb;
+      if (lane == (unsigned)l) found = f;
+    }
+    if (found) next_edges += A_off[v + 1] - A_off[v];
     const uint32_t mask = __ballot_sync(kFull, found);
     if (lane == 0) {
       fb_out[w] = mask;
@@ -633,8 +710,20 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
     }
     if (nv) {
       ProfScope ps(g, F_REACH_VGC);
-      k_reach_vgc<kVgcBlock, kVgcQueue>
-          <<<grid_for(g, v_items * 32, kVgcBlock), kVgcBlock, 0, g->stream>>>(vg[0], vg[1], tau);
+      // a resident grid; one frontier vertex per warp while the frontier
+      // fits it, else chunks of up to 32 so that every warp stays busy
+      if (!g->vgc_blocks) {
+        PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue>, kVgcBlock, 0));
+        if (g->vgc_blocks < 1) g->vgc_blocks = 1;
+      }
+      const uint64_t max_blocks = (uint64_t)g->num_sms * g->vgc_blocks;
+      const uint64_t max_warps = max_blocks * (kVgcBlock / 32);
+      const uint64_t chunk = std::min<uint64_t>(32, (v_items + max_warps - 1) / max_warps);
+      const uint64_t chunks = (v_items + chunk - 1) / chunk;
+      const uint64_t blocks = std::min(max_blocks, (chunks + kVgcBlock / 32 - 1) / (kVgcBlock / 32));
+      k_reach_vgc<kVgcBlock, kVgcQueue><<<(unsigned)std::max<uint64_t>(1, blocks), kVgcBlock, 0,
+                                          g->stream>>>(vg[0], vg[1], tau, (uint32_t)chunk);
     }
     if (np) {
       ProfScope ps(g, F_REACH_PUSH);
@@ -681,10 +770,12 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       give_event(g, tr_b);
       for (int k = 0; k < ns; k++)
         if (mode[k] != M_NONE)
-          std::fprintf(stderr, "reach side %d round %u mode %s nf %llu next %llu edges %llu t %.3f ms\n",
+          std::fprintf(stderr, "reach side %d round %u mode %s nf %llu next %llu edges %llu "
+                       "expanded %llu waves %llu t %.3f ms\n",
                        k, sides[k].rounds, mode[k] == M_VGC ? "vgc" : mode[k] == M_PUSH ? "push" : "pull",
                        (unsigned long long)sides[k].nf, g->hctr[sides[k].cset].next,
-                       g->hctr[sides[k].cset].edges, us);
+                       g->hctr[sides[k].cset].edges, g->hctr[sides[k].cset].expanded,
+                       g->hctr[sides[k].cset].waves, us);
     }
     for (int k = 0; k < ns; k++) {
       Side& s = sides[k];

@@ -142,6 +142,61 @@ int psc_scc_batch_device(psc_graph_t g, const psc_params_t* p, const uint64_t* s
  * same partition as psc_cc on each graph alone). */
 int psc_cc_batch(psc_graph_t g, double beta, uint32_t* labels_out);
 
+/* Request server: SCC and connectivity solves of independent graphs served
+ * with continuous batching under a device-memory budget.  No counterpart in
+ * the reference.
+ *
+ * Submitted requests queue in arrival order.  Each of `workers` threads (one
+ * CUDA stream each) takes, whenever it is free, the queued requests of the
+ * kind at the head of the queue while their estimated device footprint fits
+ * hbm_budget minus what running batches hold (at most max_batch requests),
+ * packs them into one batch on the device, solves it with the batched path
+ * and copies each member's labels to its caller.  Requests arriving while
+ * batches run are admitted as workers and budget free up; their work overlaps
+ * the running batches.  A request larger than the whole budget is refused at
+ * submission (PSC_ERR_TOO_LARGE).  Results do not depend on the mix: SCC
+ * labels equal psc_scc on the graph alone with p->seed = the request's seed,
+ * connectivity labels give psc_cc's partition (roots local to the graph). */
+typedef struct psc_server_s* psc_server_t;
+#define PSC_REQ_SCC 0 /* directed CSR; labels_out u64[n] as psc_scc */
+#define PSC_REQ_CC 1  /* symmetric CSR; labels_out u32[n] as psc_cc */
+typedef struct {
+  uint64_t hbm_budget;  /* device bytes admitted batches may hold (120 GiB) */
+  uint32_t workers;     /* batches in flight, one stream each (4) */
+  uint32_t max_batch;   /* requests per batch (4096) */
+  double cc_beta;       /* LDD beta of connectivity requests (0.2) */
+  psc_params_t scc;     /* SCC parameters; the seed comes with each request */
+} psc_server_config_t;
+typedef struct {
+  uint64_t submitted, completed, failed, rejected, batches;
+  uint64_t peak_bytes;    /* largest admitted footprint at one time */
+  uint64_t max_running;   /* most batches in flight at one time */
+  uint64_t queued, bytes_in_use;
+  double busy_ms;         /* sum of batch wall times over workers */
+} psc_server_stats_t;
+typedef struct {
+  int32_t status;       /* PSC_OK or the batch's error */
+  uint32_t batch_size;  /* requests solved together with this one */
+  double queue_ms;      /* submission to the start of its batch */
+  double latency_ms;    /* submission to its labels in host memory */
+} psc_request_info_t;
+void psc_server_config_default(psc_server_config_t* cfg);
+/* cfg NULL: the defaults.  The server uses the calling thread's device. */
+int psc_server_create(const psc_server_config_t* cfg, psc_server_t* out);
+/* off u64[n+1], E u32[m] and labels_out stay owned by the caller and must
+ * stay valid until psc_server_wait returns for the request's id. */
+int psc_server_submit(psc_server_t s, int kind, const uint64_t* off, const uint32_t* E, uint64_t n,
+                      uint64_t m, uint64_t seed, void* labels_out, uint64_t* id_out);
+/* Blocks until the request is done, fills info (may be NULL), forgets the id
+ * and returns the request's status. */
+int psc_server_wait(psc_server_t s, uint64_t id, psc_request_info_t* info);
+/* Blocks until nothing is queued or running. */
+int psc_server_drain(psc_server_t s);
+int psc_server_stats(psc_server_t s, psc_server_stats_t* out);
+/* Serves what is still queued, then stops the workers and frees the server;
+ * call it after the last psc_server_wait. */
+int psc_server_destroy(psc_server_t s);
+
 /* psc_reach without any memory allocation.  No counterpart in the reference.
  *
  * For callers that may not allocate device memory themselves: engines that

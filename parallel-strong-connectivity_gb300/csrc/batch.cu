@@ -47,20 +47,6 @@ constexpr uint64_t kBatchVgcMax = ~0ull;
 // Graph-offset table
 // ---------------------------------------------------------------------------
 
-// Largest k in [0, cnt) with a[k] <= x, for a nondecreasing a with a[0] <= x.
-template <class T>
-__device__ __forceinline__ uint32_t last_le(const T* __restrict__ a, uint32_t cnt, uint64_t x) {
-  uint32_t lo = 0, hi = cnt;  // a[lo] <= x, a[hi] > x (virtually for hi == cnt)
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if ((uint64_t)a[mid] <= x)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
-
 __global__ void k_fill_gid(const uint64_t* __restrict__ vbase, uint32_t G, uint64_t n, uint32_t* gid) {
   for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x)
@@ -475,7 +461,9 @@ int scc_batch_run(psc_graph_s* g, const psc_params_t* p, const uint64_t* seeds, 
 
 using namespace psc;
 
-extern "C" int psc_batch_set(psc_graph_t g, const uint64_t* vbase, uint32_t num_graphs) {
+namespace psc {
+
+int batch_attach(psc_graph_s* g, const uint64_t* vbase, uint32_t num_graphs, bool check) {
   if (!g || !vbase || num_graphs == 0) return PSC_ERR_INVALID;
   if (vbase[0] != 0 || vbase[num_graphs] != g->n) return PSC_ERR_INVALID;
   for (uint32_t k = 0; k < num_graphs; k++)
@@ -492,22 +480,31 @@ extern "C" int psc_batch_set(psc_graph_t g, const uint64_t* vbase, uint32_t num_
   PSC_CUDA(cudaMemcpyAsync(g->d_vbase, vbase, ((size_t)num_graphs + 1) * 8, cudaMemcpyHostToDevice,
                            g->stream));
   k_fill_gid<<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(g->d_vbase, num_graphs, g->n, g->d_gid);
-  PSC_CUDA(cudaMemsetAsync(&g->ctr->aux0, 0, 8, g->stream));
-  k_check_batch<<<grid_for(g, g->n * 32, 256), 256, 0, g->stream>>>(
-      g->off, g->E, g->in_off, g->in_E, g->d_vbase, g->d_gid, g->n, &g->ctr->aux0);
   PSC_CUDA(cudaGetLastError());
-  PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux0, &g->ctr->aux0, 8, cudaMemcpyDeviceToHost, g->stream));
-  PSC_CUDA(cudaStreamSynchronize(g->stream));
-  if (g->hctr->aux0 != 0) {
-    cudaFreeAsync(g->d_vbase, g->stream);
-    cudaFreeAsync(g->d_gid, g->stream);
-    g->d_vbase = nullptr;
-    g->d_gid = nullptr;
-    return PSC_ERR_INVALID;  // an edge crosses two graphs
+  if (check) {
+    PSC_CUDA(cudaMemsetAsync(&g->ctr->aux0, 0, 8, g->stream));
+    k_check_batch<<<grid_for(g, g->n * 32, 256), 256, 0, g->stream>>>(
+        g->off, g->E, g->in_off, g->in_E, g->d_vbase, g->d_gid, g->n, &g->ctr->aux0);
+    PSC_CUDA(cudaGetLastError());
+    PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux0, &g->ctr->aux0, 8, cudaMemcpyDeviceToHost, g->stream));
+    PSC_CUDA(cudaStreamSynchronize(g->stream));
+    if (g->hctr->aux0 != 0) {
+      cudaFreeAsync(g->d_vbase, g->stream);
+      cudaFreeAsync(g->d_gid, g->stream);
+      g->d_vbase = nullptr;
+      g->d_gid = nullptr;
+      return PSC_ERR_INVALID;  // an edge crosses two graphs
+    }
   }
   g->vbase.assign(vbase, vbase + num_graphs + 1);
   g->num_graphs = num_graphs;
   return PSC_OK;
+}
+
+}  // namespace psc
+
+extern "C" int psc_batch_set(psc_graph_t g, const uint64_t* vbase, uint32_t num_graphs) {
+  return batch_attach(g, vbase, num_graphs, true);
 }
 
 extern "C" uint32_t psc_batch_num_graphs(psc_graph_t g) { return g ? g->num_graphs : 0; }
@@ -543,18 +540,28 @@ extern "C" int psc_scc_batch(psc_graph_t g, const psc_params_t* p, const uint64_
   return call_end(g);
 }
 
+namespace psc {
+
+int cc_batch_run(psc_graph_s* g, double beta, uint32_t* d_labels) {
+  PSC_TRY(cc_run(g, beta, d_labels, nullptr, nullptr));
+  {
+    ProfScope ps(g, F_BATCH);
+    ps.bytes = 12.0 * g->n;
+    k_localise_u32<<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(d_labels, g->n, g->d_gid,
+                                                                 g->d_vbase);
+  }
+  PSC_CUDA(cudaGetLastError());
+  return PSC_OK;
+}
+
+}  // namespace psc
+
 extern "C" int psc_cc_batch(psc_graph_t g, double beta, uint32_t* labels_out) {
   if (!g || !labels_out || !(beta > 0) || g->num_graphs == 0) return PSC_ERR_INVALID;
   PSC_TRY(call_begin(g));
   uint32_t* d;
   PSC_TRY(ensure_t(g, B_AUX0, g->n + 1, &d));
-  PSC_TRY(cc_run(g, beta, d, nullptr, nullptr));
-  {
-    ProfScope ps(g, F_BATCH);
-    ps.bytes = 12.0 * g->n;
-    k_localise_u32<<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(d, g->n, g->d_gid, g->d_vbase);
-  }
-  PSC_CUDA(cudaGetLastError());
+  PSC_TRY(cc_batch_run(g, beta, d));
   PSC_CUDA(cudaMemcpyAsync(labels_out, d, g->n * 4, cudaMemcpyDeviceToHost, g->stream));
   return call_end(g);
 }

@@ -282,6 +282,20 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
   return v;
 }
 
+// Largest k in [0, cnt) with a[k] <= x, for a nondecreasing a with a[0] <= x.
+template <class T>
+__device__ __forceinline__ uint32_t last_le(const T* __restrict__ a, uint32_t cnt, uint64_t x) {
+  uint32_t lo = 0, hi = cnt;  // a[lo] <= x, a[hi] > x (virtually for hi == cnt)
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if ((uint64_t)a[mid] <= x)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 // Per-warp shared state of the balanced expansion.
 struct WarpExpandSmem {
   uint32_t excl[32];

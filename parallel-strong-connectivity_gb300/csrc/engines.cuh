@@ -5,6 +5,15 @@
 namespace psc {
 
 int ensure_keep(psc_graph_s* g, int b, size_t bytes, size_t keep, void** out);
+// A handle with its stream, counters and events for a graph of n vertices
+// and m edges, and its graph arrays from the stream-ordered pool
+// (in_off/in_E alias off/E when symmetric).
+int make_handle(uint64_t n, uint64_t m, psc_graph_s** out);
+int alloc_graph_arrays(psc_graph_s* g, bool symmetric);
+// Attaches a graph-offset table (vertex bases, host u64[G+1]) to g: the
+// per-vertex graph ids and, when check is set, the test that no edge crosses
+// two graphs.
+int batch_attach(psc_graph_s* g, const uint64_t* vbase, uint32_t num_graphs, bool check);
 int call_begin(psc_graph_s* g);
 int call_end(psc_graph_s* g);
 
@@ -73,5 +82,8 @@ int scc_batch_run(psc_graph_s* g, const psc_params_t* p, const uint64_t* seeds, 
 
 // Connectivity labels u32[n] of the union (cc.cu).
 int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, uint64_t* n_forest);
+
+// Connectivity of every graph of a batch: component roots local to each graph.
+int cc_batch_run(psc_graph_s* g, double beta, uint32_t* d_labels);
 
 }  // namespace psc

@@ -161,7 +161,7 @@ int call_end(psc_graph_s* g) {
   return PSC_OK;
 }
 
-static int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
+int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
   int dev = 0;
   PSC_CUDA(cudaGetDevice(&dev));
   auto* g = new psc_graph_s();
@@ -193,7 +193,7 @@ static int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
 
 // Graph arrays come from the device's stream-ordered pool (kept between
 // handles), so repeated uploads of same-sized graphs do not map new memory.
-static int alloc_graph_arrays(psc_graph_s* g, bool symmetric) {
+int alloc_graph_arrays(psc_graph_s* g, bool symmetric) {
   const uint64_t n = g->n, m = g->m;
   g->symmetric = symmetric;
   PSC_CUDA(cudaMallocAsync((void**)&g->off, (n + 1) * sizeof(uint64_t), g->stream));

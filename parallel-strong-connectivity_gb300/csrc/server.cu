@@ -1,0 +1,343 @@
+// Request server: SCC and connectivity solves of many independent graphs
+// served with continuous batching under a device-memory budget.  No
+// counterpart in the reference, whose drivers solve one graph per process
+// (src/scc.cpp:57-67, src/Connectivity.cpp:28-33).
+//
+// Requests wait in one FIFO queue.  Each of `workers` threads owns a CUDA
+// stream; whenever it is free it admits, in arrival order, the queued
+// requests of the kind at the head of the queue while their estimated device
+// footprint fits the budget left by the batches still running, packs them
+// into one disjoint-union graph on the device (the members' CSR arrays are
+// copied into slices and rebased by one kernel; the transpose of an SCC batch
+// is built on the device), solves the batch with the lockstep batched
+// SCC / connectivity path, copies every member's labels to its caller and
+// releases the memory.  Requests that arrive while batches are running are
+// admitted as soon as a worker and enough budget are free, so their work
+// overlaps the running batches on the device.
+//
+// A request's result does not depend on the batch it lands in: SCC labels
+// equal psc_scc on the graph alone with the request's seed, connectivity
+// labels give the same partition as psc_cc on the graph alone.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "common.cuh"
+#include "engines.cuh"
+
+namespace psc {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  uint64_t id = 0;
+  int kind = PSC_REQ_SCC;
+  uint64_t n = 0, m = 0;
+  const uint64_t* off = nullptr;
+  const uint32_t* E = nullptr;
+  uint64_t seed = 0;
+  void* out = nullptr;
+  uint64_t bytes = 0;
+  Clock::time_point t_submit, t_start, t_done;
+  bool done = false;
+  int status = PSC_OK;
+  uint32_t batch_size = 0;
+};
+
+// Device bytes a request may need while its batch runs: graph arrays (and the
+// transpose with its build scratch for SCC), labels and the solver's scratch
+// (pivot order, queues, bitmaps, label tables) per vertex.
+uint64_t request_bytes(int kind, uint64_t n, uint64_t m) {
+  if (kind == PSC_REQ_SCC) return 16 * (n + 1) + 12 * m + 160 * n;
+  return 8 * (n + 1) + 4 * m + 64 * n;
+}
+
+__global__ void k_rebase(uint64_t* off, uint64_t n, uint32_t* E, uint64_t m,
+                         const uint64_t* __restrict__ vbase, const uint64_t* __restrict__ ebase,
+                         uint32_t R) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n + m;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    if (i < n) {
+      off[i] += ebase[last_le(vbase, R, i)];
+    } else {
+      const uint64_t j = i - n;
+      E[j] += (uint32_t)vbase[last_le(ebase, R, j)];
+    }
+  }
+}
+
+__global__ void k_put_u64(uint64_t* p, uint64_t v) { *p = v; }
+
+}  // namespace
+}  // namespace psc
+
+struct psc_server_s {
+  psc_server_config_t cfg{};
+  int device = 0;
+  std::mutex mu;
+  std::condition_variable work_cv;  // queue or budget changed
+  std::condition_variable done_cv;  // a request completed
+  std::deque<psc::Request*> queue;
+  std::unordered_map<uint64_t, psc::Request*> requests;
+  std::vector<std::thread> workers;
+  uint64_t next_id = 1;
+  uint64_t used = 0;      // bytes admitted by running batches
+  uint32_t running = 0;   // batches on the device
+  bool stop = false;
+  psc_server_stats_t stats{};
+};
+
+namespace psc {
+namespace {
+
+// Solves one batch of requests of the same kind on a fresh handle.
+int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind) {
+  const uint32_t R = (uint32_t)B.size();
+  std::vector<uint64_t> vbase(R + 1, 0), ebase(R + 1, 0);
+  for (uint32_t k = 0; k < R; k++) {
+    vbase[k + 1] = vbase[k] + B[k]->n;
+    ebase[k + 1] = ebase[k] + B[k]->m;
+  }
+  const uint64_t n = vbase[R], m = ebase[R];
+  if (n >= 0xFFFFFFFFull) return PSC_ERR_TOO_LARGE;
+  psc_graph_s* g = nullptr;
+  PSC_TRY(make_handle(n, m, &g));
+  auto body = [&]() -> int {
+    PSC_TRY(alloc_graph_arrays(g, kind == PSC_REQ_CC));
+    PSC_TRY(call_begin(g));
+    for (uint32_t k = 0; k < R; k++) {
+      PSC_CUDA(cudaMemcpyAsync(g->off + vbase[k], B[k]->off, B[k]->n * 8, cudaMemcpyDefault, g->stream));
+      if (B[k]->m)
+        PSC_CUDA(cudaMemcpyAsync(g->E + ebase[k], B[k]->E, B[k]->m * 4, cudaMemcpyDefault, g->stream));
+    }
+    uint64_t* bases;
+    PSC_TRY(ensure_t(g, B_SCHED, 2 * (size_t)R + 2, &bases));
+    std::vector<uint64_t> hb(2 * (size_t)R + 2);
+    std::copy(vbase.begin(), vbase.end(), hb.begin());
+    std::copy(ebase.begin(), ebase.end(), hb.begin() + R + 1);
+    PSC_CUDA(cudaMemcpyAsync(bases, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    k_rebase<<<grid_for(g, n + m, 256), 256, 0, g->stream>>>(g->off, n, g->E, m, bases, bases + R + 1,
+                                                              R);
+    k_put_u64<<<1, 1, 0, g->stream>>>(g->off + n, m);
+    PSC_CUDA(cudaGetLastError());
+    if (kind == PSC_REQ_SCC) PSC_TRY(build_transpose(g));
+    PSC_TRY(batch_attach(g, vbase.data(), R, false));
+    if (kind == PSC_REQ_SCC) {
+      uint64_t* d;
+      PSC_TRY(ensure_t(g, B_LABELS, n, &d));
+      std::vector<uint64_t> seeds(R);
+      for (uint32_t k = 0; k < R; k++) seeds[k] = B[k]->seed;
+      PSC_TRY(scc_batch_run(g, &S->cfg.scc, seeds.data(), d));
+      for (uint32_t k = 0; k < R; k++)
+        PSC_CUDA(cudaMemcpyAsync(B[k]->out, d + vbase[k], B[k]->n * 8, cudaMemcpyDefault, g->stream));
+    } else {
+      uint32_t* d;
+      PSC_TRY(ensure_t(g, B_AUX0, n + 1, &d));
+      PSC_TRY(cc_batch_run(g, S->cfg.cc_beta, d));
+      for (uint32_t k = 0; k < R; k++)
+        PSC_CUDA(cudaMemcpyAsync(B[k]->out, d + vbase[k], B[k]->n * 4, cudaMemcpyDefault, g->stream));
+    }
+    return call_end(g);
+  };
+  const int st = body();
+  psc_graph_free(g);
+  return st;
+}
+
+// Batch of the queue head's kind: requests in arrival order while they fit
+// the budget left (a lone request always fits an idle server).  Caller holds
+// the lock.  Returns false if nothing may start now.
+bool take_batch(psc_server_s* S, std::vector<Request*>& batch, int& kind, uint64_t& bytes) {
+  if (S->queue.empty()) return false;
+  const uint64_t budget = S->cfg.hbm_budget;
+  kind = S->queue.front()->kind;
+  bytes = 0;
+  for (auto it = S->queue.begin(); it != S->queue.end() && batch.size() < S->cfg.max_batch;) {
+    Request* r = *it;
+    if (r->kind != kind) {
+      ++it;
+      continue;
+    }
+    const bool fits = S->used + bytes + r->bytes <= budget;
+    if (!fits && !(batch.empty() && S->running == 0)) break;
+    batch.push_back(r);
+    bytes += r->bytes;
+    it = S->queue.erase(it);
+  }
+  return !batch.empty();
+}
+
+void worker_loop(psc_server_s* S) {
+  cudaSetDevice(S->device);
+  for (;;) {
+    std::vector<Request*> batch;
+    int kind = 0;
+    uint64_t bytes = 0;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      // on stop, the queue is still served before the workers leave
+      S->work_cv.wait(lk, [&] { return take_batch(S, batch, kind, bytes) || S->stop; });
+      if (batch.empty()) return;  // stopping with nothing to take
+      S->used += bytes;
+      S->running++;
+      S->stats.batches++;
+      S->stats.peak_bytes = std::max(S->stats.peak_bytes, S->used);
+      S->stats.max_running = std::max<uint64_t>(S->stats.max_running, S->running);
+    }
+    const auto t0 = Clock::now();
+    for (auto* r : batch) {
+      r->t_start = t0;
+      r->batch_size = (uint32_t)batch.size();
+    }
+    const int st = run_batch(S, batch, kind);
+    const auto t1 = Clock::now();
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->used -= bytes;
+      S->running--;
+      S->stats.busy_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+      for (auto* r : batch) {
+        r->t_done = t1;
+        r->status = st;
+        r->done = true;
+        S->stats.completed++;
+        if (st != PSC_OK) S->stats.failed++;
+      }
+    }
+    S->done_cv.notify_all();
+    S->work_cv.notify_all();
+  }
+}
+
+}  // namespace
+}  // namespace psc
+
+using namespace psc;
+
+extern "C" void psc_server_config_default(psc_server_config_t* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->hbm_budget = 120ull << 30;
+  c->workers = 4;
+  c->max_batch = 4096;
+  c->cc_beta = 0.2;
+  psc_params_default(&c->scc);
+}
+
+extern "C" int psc_server_create(const psc_server_config_t* cfg, psc_server_t* out) {
+  if (!out) return PSC_ERR_INVALID;
+  *out = nullptr;
+  psc_server_config_t c;
+  psc_server_config_default(&c);
+  if (cfg) c = *cfg;
+  if (c.hbm_budget == 0 || c.workers == 0 || c.workers > 64 || c.max_batch == 0 ||
+      !(c.cc_beta > 0) || !(c.scc.beta > 0))
+    return PSC_ERR_INVALID;
+  int dev = 0;
+  PSC_CUDA(cudaGetDevice(&dev));
+  auto* S = new psc_server_s();
+  S->cfg = c;
+  S->device = dev;
+  for (uint32_t w = 0; w < c.workers; w++) S->workers.emplace_back(worker_loop, S);
+  *out = S;
+  return PSC_OK;
+}
+
+extern "C" int psc_server_submit(psc_server_t S, int kind, const uint64_t* off, const uint32_t* E,
+                                 uint64_t n, uint64_t m, uint64_t seed, void* labels_out,
+                                 uint64_t* id_out) {
+  if (!S || !off || (m && !E) || !labels_out || !id_out || n == 0 || n >= 0xFFFFFFFFull)
+    return PSC_ERR_INVALID;
+  if (kind != PSC_REQ_SCC && kind != PSC_REQ_CC) return PSC_ERR_INVALID;
+  if (off[0] != 0 || off[n] != m) return PSC_ERR_INVALID;
+  const uint64_t bytes = request_bytes(kind, n, m);
+  auto* r = new Request();
+  r->kind = kind;
+  r->n = n;
+  r->m = m;
+  r->off = off;
+  r->E = E;
+  r->seed = seed;
+  r->out = labels_out;
+  r->bytes = bytes;
+  r->t_submit = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stop) {
+      delete r;
+      return PSC_ERR_INVALID;
+    }
+    if (bytes > S->cfg.hbm_budget) {
+      S->stats.rejected++;
+      delete r;
+      return PSC_ERR_TOO_LARGE;
+    }
+    r->id = S->next_id++;
+    S->requests[r->id] = r;
+    S->queue.push_back(r);
+    S->stats.submitted++;
+    *id_out = r->id;
+  }
+  S->work_cv.notify_one();
+  return PSC_OK;
+}
+
+extern "C" int psc_server_wait(psc_server_t S, uint64_t id, psc_request_info_t* info) {
+  if (!S) return PSC_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->requests.find(id);
+  if (it == S->requests.end()) return PSC_ERR_INVALID;
+  Request* r = it->second;
+  S->done_cv.wait(lk, [&] { return r->done; });
+  if (info) {
+    info->status = r->status;
+    info->batch_size = r->batch_size;
+    info->queue_ms = std::chrono::duration<double, std::milli>(r->t_start - r->t_submit).count();
+    info->latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  }
+  const int st = r->status;
+  S->requests.erase(it);
+  delete r;
+  return st;
+}
+
+extern "C" int psc_server_drain(psc_server_t S) {
+  if (!S) return PSC_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(S->mu);
+  S->done_cv.wait(lk, [&] {
+    if (!S->queue.empty() || S->running) return false;
+    for (auto& kv : S->requests)
+      if (!kv.second->done) return false;
+    return true;
+  });
+  return PSC_OK;
+}
+
+extern "C" int psc_server_stats(psc_server_t S, psc_server_stats_t* out) {
+  if (!S || !out) return PSC_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(S->mu);
+  *out = S->stats;
+  out->queued = S->queue.size();
+  out->bytes_in_use = S->used;
+  return PSC_OK;
+}
+
+extern "C" int psc_server_destroy(psc_server_t S) {
+  if (!S) return PSC_OK;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->work_cv.notify_all();
+  for (auto& t : S->workers) t.join();
+  for (auto& kv : S->requests) delete kv.second;
+  delete S;
+  return PSC_OK;
+}

@@ -7,3 +7,4 @@ libpsc_host.so and exposes the calls.  There is no CPU fallback.
 from ._lib import Params, PscError, Stats, cuda, host, strerror  # noqa: F401
 from .graph import (DeviceGraph, HostGraph, batch_member, batch_member_spec,  # noqa: F401
                     batch_workload, default_params, random_permutation)
+from .server import Server, server_config  # noqa: F401

@@ -59,6 +59,34 @@ class Stats(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    """psc_server_config_t (include/psc.h)."""
+    _fields_ = [
+        ("hbm_budget", C.c_uint64),
+        ("workers", C.c_uint32),
+        ("max_batch", C.c_uint32),
+        ("cc_beta", C.c_double),
+        ("scc", Params),
+    ]
+
+
+class ServerStats(C.Structure):
+    """psc_server_stats_t (include/psc.h)."""
+    _fields_ = [(f, C.c_uint64) for f in ("submitted", "completed", "failed", "rejected", "batches",
+                                          "peak_bytes", "max_running", "queued", "bytes_in_use")] + \
+        [("busy_ms", C.c_double)]
+
+
+class RequestInfo(C.Structure):
+    """psc_request_info_t (include/psc.h)."""
+    _fields_ = [
+        ("status", C.c_int32),
+        ("batch_size", C.c_uint32),
+        ("queue_ms", C.c_double),
+        ("latency_ms", C.c_double),
+    ]
+
+
 P = C.c_void_p
 U64 = C.c_uint64
 U32 = C.c_uint32
@@ -88,6 +116,13 @@ CUDA_SIGNATURES = {
     "psc_scc_batch": (I32, [P, C.POINTER(Params), P, P]),
     "psc_scc_batch_device": (I32, [P, C.POINTER(Params), P, P]),
     "psc_cc_batch": (I32, [P, D, P]),
+    "psc_server_config_default": (None, [C.POINTER(ServerConfig)]),
+    "psc_server_create": (I32, [C.POINTER(ServerConfig), C.POINTER(P)]),
+    "psc_server_submit": (I32, [P, I32, P, P, U64, U64, U64, P, C.POINTER(U64)]),
+    "psc_server_wait": (I32, [P, U64, C.POINTER(RequestInfo)]),
+    "psc_server_drain": (I32, [P]),
+    "psc_server_stats": (I32, [P, C.POINTER(ServerStats)]),
+    "psc_server_destroy": (I32, [P]),
     "psc_last_stats": (I32, [P, C.POINTER(Stats)]),
     "psc_set_profiling": (I32, [P, I32]),
     "psc_profile_count": (I32, []),

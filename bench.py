@@ -457,6 +457,207 @@ def run_batch(args, world, rank, local, dist) -> None:
     print(json.dumps(line), flush=True)
 
 
+SERVE = dict(pool=48, seed0=5000, log10_min=3.0, log10_max=7.0, cc_share=0.2,
+             rates=(200, 1000, 5000), requests=240, budget=120 << 30)
+
+
+def serve_pool(psc, count: int, seed0: int):
+    """Seeded request pool: member i has n = floor(10^u) vertices, u uniform
+    in [3, 7) drawn from seed0 + i; even members R-MAT (2^round(log2 n)
+    vertices, 16 draws per vertex), odd members 2-D kNN (k = 5)."""
+    import math
+    out = []
+    for i in range(count):
+        u = SERVE["log10_min"] + (SERVE["log10_max"] - SERVE["log10_min"]) * _unit(seed0 + i)
+        n = int(10 ** u)
+        if i % 2 == 0:
+            log2n = max(8, round(math.log2(n)))
+            out.append(psc.HostGraph.rmat(log2n, 16 << log2n, seed=seed0 + i))
+        else:
+            out.append(psc.HostGraph.knn(max(n, 16), 5, seed=seed0 + i))
+    return out
+
+
+def _unit(seed: int) -> float:
+    """Uniform [0, 1) draw of a seed (SplitMix64 finaliser of the seed)."""
+    x = (seed + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    x ^= x >> 30
+    x = (x * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    x ^= x >> 27
+    x = (x * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    x ^= x >> 31
+    return (x >> 11) / float(1 << 53)
+
+
+def run_serve(args, world, rank, local, dist) -> None:
+    """Served stream: Poisson arrivals of SCC (80 %) and connectivity (20 %)
+    requests drawn from a seeded pool, through the request server
+    (continuous batching, 120 GiB admission budget); latency p50/p99 and
+    graphs/s per arrival rate, against the same requests solved one by one
+    with plain calls."""
+    import threading
+    import psc
+    from psc import _lib
+    from psc.server import CC, SCC
+
+    lib = psc.cuda()
+    if world > 1:
+        _lib.check(lib.psc_set_device(local), "psc_set_device")
+    t = time.perf_counter()
+    pool = serve_pool(psc, SERVE["pool"], SERVE["seed0"])
+    rng = np.random.default_rng(SERVE["seed0"])
+    nreq = args.serve_requests
+    picks = rng.integers(0, len(pool), nreq)
+    kinds = np.where(rng.random(nreq) < SERVE["cc_share"], CC, SCC)
+    sym = {}
+    for i in sorted(set(picks[kinds == CC].tolist())):
+        sym[i] = pool[i].symmetrize()
+    # pinned copies of the request arrays (what a serving front end holds)
+    pin = Pinned(lib)
+    parr = {}
+    for i in set(picks.tolist()):
+        for kind in (SCC, CC):
+            if kind == CC and i not in sym:
+                continue
+            g = pool[i] if kind == SCC else sym[i]
+            parr[(i, kind)] = (g, pin.copy(g.off), pin.copy(g.E) if g.m else g.E)
+    ptr_t = {i: (pool[i], pin.copy(pool[i].in_off), pin.copy(pool[i].in_E) if pool[i].m else
+                 pool[i].in_E) for i in set(picks[kinds == SCC].tolist())}
+    log(f"[rank {rank}] serve pool of {len(pool)} graphs (n {min(g.n for g in pool)}.."
+        f"{max(g.n for g in pool)}) built in {time.perf_counter() - t:.1f}s")
+    seeds = (1000 + np.arange(nreq)).astype(np.uint64)
+
+    def request(j):
+        g, off, E = parr[(int(picks[j]), int(kinds[j]))]
+        return g, off, E, int(kinds[j]), int(seeds[j])
+
+    def submit(srv, j, out):
+        # requests carry the graph as struct Graph does: CSR and, for SCC,
+        # its transpose
+        g, off, E, kind, seed = request(j)
+        tin = (ptr_t[int(picks[j])][1].ctypes.data, ptr_t[int(picks[j])][2].ctypes.data) \
+            if kind == SCC else (None, None)
+        rid = C.c_uint64()
+        _lib.check(lib.psc_server_submit(srv, kind, off.ctypes.data, E.ctypes.data, tin[0], tin[1],
+                                         g.n, g.m, seed, out.ctypes.data, C.byref(rid)),
+                   "psc_server_submit")
+        return rid.value
+
+    outs = [pin.empty(request(j)[0].n, np.uint64 if kinds[j] == SCC else np.uint32)
+            for j in range(nreq)]
+
+    def serve(rate: float | None) -> dict:
+        cfg = psc.server_config(hbm_budget=SERVE["budget"], workers=args.serve_workers)
+        h = C.c_void_p()
+        _lib.check(lib.psc_server_create(C.byref(cfg), C.byref(h)), "psc_server_create")
+        arr = np.cumsum(rng.exponential(1.0 / rate, nreq)) if rate else np.zeros(nreq)
+        ids = [None] * nreq
+        lat = np.zeros(nreq)
+        done_t = np.zeros(nreq)
+        ready = threading.Event()
+
+        def waiter():
+            ready.wait()
+            for j in range(nreq):
+                while ids[j] is None:
+                    time.sleep(0.0002)
+                info = _lib.RequestInfo()
+                _lib.check(lib.psc_server_wait(h, ids[j], C.byref(info)), "psc_server_wait")
+                lat[j] = info.latency_ms
+                done_t[j] = time.perf_counter()
+
+        wt = threading.Thread(target=waiter)
+        wt.start()
+        t0 = time.perf_counter()
+        ready.set()
+        for j in range(nreq):
+            d = t0 + arr[j] - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            ids[j] = submit(h, j, outs[j])
+        wt.join()
+        st = _lib.ServerStats()
+        lib.psc_server_stats(h, C.byref(st))
+        lib.psc_server_destroy(h)
+        span = done_t.max() - t0
+        return {"rate": rate, "graphs_per_s": nreq / span, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "batches": int(st.batches),
+                "max_in_flight": int(st.max_running), "peak_gb": st.peak_bytes / 1e9,
+                "launches": int(st.kernel_launches)}
+
+    serve(None)  # warm-up (pool allocations, module load)
+    # reference results of the mixed stream for the equality check
+    sweep = []
+    with ClockSampler(local) as clk:
+        for rate in SERVE["rates"]:
+            sweep.append(serve(float(rate)))
+            log(f"  rate {rate}/s: {sweep[-1]}")
+        sat = serve(None)
+    clocks = clk.summary()
+    mixed = [o.copy() for o in outs]
+
+    # plain sequential solves of the same stream
+    t = time.perf_counter()
+    for j in range(nreq):
+        g, off, E, kind, seed = request(j)
+        h = C.c_void_p()
+        if kind == SCC:
+            # the host-built transpose is uploaded too (not timed to build)
+            _, in_off, in_E = ptr_t[int(picks[j])]
+            _lib.check(lib.psc_graph_upload(off.ctypes.data, E.ctypes.data, in_off.ctypes.data,
+                                            in_E.ctypes.data, g.n, g.m, C.byref(h)), "upload")
+            p = psc.default_params(seed=seed)
+            _lib.check(lib.psc_scc(h, C.byref(p), outs[j].ctypes.data), "psc_scc")
+        else:
+            _lib.check(lib.psc_graph_upload(off.ctypes.data, E.ctypes.data, None, None, g.n, g.m,
+                                            C.byref(h)), "upload")
+            _lib.check(lib.psc_cc(h, 0.2, outs[j].ctypes.data, None, None), "psc_cc")
+        lib.psc_graph_free(h)
+    plain_s = time.perf_counter() - t
+    bad = 0
+    for j in range(nreq):
+        if kinds[j] == SCC:
+            bad += not np.array_equal(outs[j], mixed[j])
+        else:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import pyoracle
+            bad += not np.array_equal(pyoracle.canon(outs[j]), pyoracle.canon(mixed[j]))
+    if bad:
+        raise SystemExit(f"{bad} served results differ from plain solves")
+    plain_rate = nreq / plain_s
+    pin.free()
+    if rank != 0:
+        return
+    top = sweep[-1]
+    line = {
+        "metric": "served SCC/CC graphs/s", "value": sat["graphs_per_s"], "unit": "graphs/s",
+        "n_gpus": world, "steps": len(SERVE["rates"]) + 1, "warmup": 1,
+        "ms_per_step": 1e3 * nreq / sat["graphs_per_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "serve", "requests_per_rate": nreq,
+                   "graph": "pool of 48 seeded graphs, n = floor(10^u), u uniform in [3, 7); even "
+                            "R-MAT (16 draws per vertex), odd 2-D kNN k=5; 80 % SCC (directed), "
+                            "20 % connectivity (symmetrised); Poisson arrivals",
+                   "hbm_budget_gb": SERVE["budget"] / 2**30, "workers": args.serve_workers,
+                   "parallelism": f"replicas{world}"},
+        "sweep": sweep, "saturated": sat,
+        "latency_ms": {"p50": top["p50_ms"], "p99": top["p99_ms"], "rate": top["rate"]},
+        "plain": {"value": plain_rate, "unit": "graphs/s",
+                  "how": "the same requests one by one from pinned memory: upload (SCC: CSR and "
+                         "its host-built transpose), psc_scc or psc_cc, labels to host, free; "
+                         "results equal the served ones"},
+        "speedup_vs_plain": sat["graphs_per_s"] / plain_rate,
+        "e2e": {"value": sat["graphs_per_s"], "unit": "graphs/s",
+                "h2d_bytes_per_step": int(sum((2 if kinds[j] == SCC else 1) *
+                                              (request(j)[0].off.nbytes + request(j)[0].E.nbytes)
+                                              for j in range(nreq))),
+                "d2h_bytes_per_step": int(sum(o.nbytes for o in outs))},
+        "roofline": None, "cpu_baseline": None, "clocks": clocks,
+        "gpu_launches": sat["launches"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
@@ -617,7 +818,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["psc", "reference"], default="psc")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="knn")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "serve"], default="knn")
+    ap.add_argument("--serve-requests", type=int, default=SERVE["requests"],
+                    help="requests per arrival rate of the serve workload")
+    ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--batch-count", type=int, default=4096,
                     help="graphs in the batch workload")
     ap.add_argument("--plain-sample", type=int, default=256,
@@ -638,6 +842,8 @@ def main():
             run_reference(args, world, rank, dist)
         elif args.workload == "batch":
             run_batch(args, world, rank, local, dist)
+        elif args.workload == "serve":
+            run_serve(args, world, rank, local, dist)
         else:
             run_gpu(args, world, rank, local, dist)
     finally:

@@ -172,6 +172,7 @@ typedef struct {
   uint64_t peak_bytes;    /* largest admitted footprint at one time */
   uint64_t max_running;   /* most batches in flight at one time */
   uint64_t queued, bytes_in_use;
+  uint64_t kernel_launches; /* kernels launched by completed batches */
   double busy_ms;         /* sum of batch wall times over workers */
 } psc_server_stats_t;
 typedef struct {
@@ -183,10 +184,13 @@ typedef struct {
 void psc_server_config_default(psc_server_config_t* cfg);
 /* cfg NULL: the defaults.  The server uses the calling thread's device. */
 int psc_server_create(const psc_server_config_t* cfg, psc_server_t* out);
-/* off u64[n+1], E u32[m] and labels_out stay owned by the caller and must
- * stay valid until psc_server_wait returns for the request's id. */
-int psc_server_submit(psc_server_t s, int kind, const uint64_t* off, const uint32_t* E, uint64_t n,
-                      uint64_t m, uint64_t seed, void* labels_out, uint64_t* id_out);
+/* off u64[n+1], E u32[m] (and for SCC optionally the transpose in_off /
+ * in_E, as struct Graph carries it; built on the device when NULL) and
+ * labels_out stay owned by the caller and must stay valid until
+ * psc_server_wait returns for the request's id. */
+int psc_server_submit(psc_server_t s, int kind, const uint64_t* off, const uint32_t* E,
+                      const uint64_t* in_off, const uint32_t* in_E, uint64_t n, uint64_t m,
+                      uint64_t seed, void* labels_out, uint64_t* id_out);
 /* Blocks until the request is done, fills info (may be NULL), forgets the id
  * and returns the request's status. */
 int psc_server_wait(psc_server_t s, uint64_t id, psc_request_info_t* info);

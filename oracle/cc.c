@@ -111,6 +111,7 @@ static uint64_t ldd_sparse(ldd_t* d, uint32_t* label) { /* ldd.hpp:88-161 */
             orc_vec_push(bag, u);
           } else {
             uint32_t lu = orc_load32(&label[u]);
+            if (lu == ORC_NMAX) continue; /* unlabelled: nothing to pass on */
             for (uint64_t j = off[u]; j < off[u + 1]; j++) {
               uint32_t v = E[j];
               if (orc_load32(&label[v]) == ORC_NMAX && orc_cas32(&label[v], ORC_NMAX, lu)) {
@@ -146,6 +147,12 @@ static uint64_t ldd_sparse(ldd_t* d, uint32_t* label) { /* ldd.hpp:88-161 */
   return orc_vec_gather(d->bag, d->nt, d->front);
 }
 
+/* Like the reference, a vertex labelled in this round joins the current
+ * frontier at once (in_frontier[i] = true, ldd.hpp:227), so later vertices of
+ * the same round may take its label.  The label is stored before the flag
+ * with release order and read after the flag with acquire order: with relaxed
+ * orders a weakly ordered CPU (Arm) can show the flag before the label, and a
+ * vertex would copy the "unlabelled" value. */
 static uint64_t ldd_dense(ldd_t* d, uint32_t* label) { /* ldd.hpp:163-247 (symmetric) */
   uint64_t cnt = 0;
 #pragma omp parallel for schedule(dynamic, LDD_BLOCK) reduction(+ : cnt) num_threads(d->nt)
@@ -154,9 +161,11 @@ static uint64_t ldd_dense(ldd_t* d, uint32_t* label) { /* ldd.hpp:163-247 (symme
     if (orc_load32(&label[i]) == ORC_NMAX) {
       for (uint64_t j = d->off[i]; j < d->off[i + 1]; j++) {
         uint32_t v = d->E[j];
-        if (orc_load8(&d->in_frontier[v])) {
-          __atomic_store_n(&label[i], orc_load32(&label[v]), __ATOMIC_RELAXED);
-          __atomic_store_n(&d->in_frontier[i], 1, __ATOMIC_RELAXED);
+        if (__atomic_load_n(&d->in_frontier[v], __ATOMIC_ACQUIRE)) {
+          const uint32_t lv = orc_load32(&label[v]);
+          if (lv == ORC_NMAX) continue;
+          __atomic_store_n(&label[i], lv, __ATOMIC_RELAXED);
+          __atomic_store_n(&d->in_frontier[i], 1, __ATOMIC_RELEASE);
           d->in_next[i] = 1;
           cnt++;
           break;

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -42,6 +43,8 @@ struct Request {
   uint64_t n = 0, m = 0;
   const uint64_t* off = nullptr;
   const uint32_t* E = nullptr;
+  const uint64_t* in_off = nullptr;  // transpose of an SCC request (optional)
+  const uint32_t* in_E = nullptr;
   uint64_t seed = 0;
   void* out = nullptr;
   uint64_t bytes = 0;
@@ -58,6 +61,9 @@ uint64_t request_bytes(int kind, uint64_t n, uint64_t m) {
   if (kind == PSC_REQ_SCC) return 16 * (n + 1) + 12 * m + 160 * n;
   return 8 * (n + 1) + 4 * m + 64 * n;
 }
+
+// Adds the batch's vertex / edge bases to the packed arrays (one request's
+// slice each: offsets get its edge base, targets its vertex base).
 
 __global__ void k_rebase(uint64_t* off, uint64_t n, uint32_t* E, uint64_t m,
                          const uint64_t* __restrict__ vbase, const uint64_t* __restrict__ ebase,
@@ -98,7 +104,7 @@ namespace psc {
 namespace {
 
 // Solves one batch of requests of the same kind on a fresh handle.
-int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind) {
+int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* launches) {
   const uint32_t R = (uint32_t)B.size();
   std::vector<uint64_t> vbase(R + 1, 0), ebase(R + 1, 0);
   for (uint32_t k = 0; k < R; k++) {
@@ -107,15 +113,36 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind) {
   }
   const uint64_t n = vbase[R], m = ebase[R];
   if (n >= 0xFFFFFFFFull) return PSC_ERR_TOO_LARGE;
+  const bool tr = trace_on();
+  std::vector<std::pair<const char*, double>> marks;
+  const auto t_begin = Clock::now();
   psc_graph_s* g = nullptr;
   PSC_TRY(make_handle(n, m, &g));
+  auto stamp = [&](const char* what) -> int {
+    if (!tr) return PSC_OK;
+    PSC_CUDA(cudaStreamSynchronize(g->stream));
+    marks.emplace_back(what, std::chrono::duration<double, std::milli>(Clock::now() - t_begin).count());
+    return PSC_OK;
+  };
   auto body = [&]() -> int {
+    PSC_TRY(stamp("handle"));
     PSC_TRY(alloc_graph_arrays(g, kind == PSC_REQ_CC));
     PSC_TRY(call_begin(g));
+    PSC_TRY(stamp("alloc"));
+    // every SCC request brought its transpose: copy it instead of building
+    bool with_t = kind == PSC_REQ_SCC;
+    for (uint32_t k = 0; k < R; k++) with_t = with_t && B[k]->in_off != nullptr;
     for (uint32_t k = 0; k < R; k++) {
       PSC_CUDA(cudaMemcpyAsync(g->off + vbase[k], B[k]->off, B[k]->n * 8, cudaMemcpyDefault, g->stream));
       if (B[k]->m)
         PSC_CUDA(cudaMemcpyAsync(g->E + ebase[k], B[k]->E, B[k]->m * 4, cudaMemcpyDefault, g->stream));
+      if (with_t) {
+        PSC_CUDA(cudaMemcpyAsync(g->in_off + vbase[k], B[k]->in_off, B[k]->n * 8, cudaMemcpyDefault,
+                                 g->stream));
+        if (B[k]->m)
+          PSC_CUDA(cudaMemcpyAsync(g->in_E + ebase[k], B[k]->in_E, B[k]->m * 4, cudaMemcpyDefault,
+                                   g->stream));
+      }
     }
     uint64_t* bases;
     PSC_TRY(ensure_t(g, B_SCHED, 2 * (size_t)R + 2, &bases));
@@ -126,37 +153,57 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind) {
     k_rebase<<<grid_for(g, n + m, 256), 256, 0, g->stream>>>(g->off, n, g->E, m, bases, bases + R + 1,
                                                               R);
     k_put_u64<<<1, 1, 0, g->stream>>>(g->off + n, m);
+    if (with_t) {
+      k_rebase<<<grid_for(g, n + m, 256), 256, 0, g->stream>>>(g->in_off, n, g->in_E, m, bases,
+                                                                bases + R + 1, R);
+      k_put_u64<<<1, 1, 0, g->stream>>>(g->in_off + n, m);
+    }
     PSC_CUDA(cudaGetLastError());
-    if (kind == PSC_REQ_SCC) PSC_TRY(build_transpose(g));
+    PSC_TRY(stamp("upload"));
+    // SCC needs the in-edges (not their order) when they did not come along
+    if (kind == PSC_REQ_SCC && !with_t) PSC_TRY(build_transpose(g, false));
     PSC_TRY(batch_attach(g, vbase.data(), R, false));
+    PSC_TRY(stamp("transpose"));
     if (kind == PSC_REQ_SCC) {
       uint64_t* d;
       PSC_TRY(ensure_t(g, B_LABELS, n, &d));
       std::vector<uint64_t> seeds(R);
       for (uint32_t k = 0; k < R; k++) seeds[k] = B[k]->seed;
       PSC_TRY(scc_batch_run(g, &S->cfg.scc, seeds.data(), d));
+      PSC_TRY(stamp("solve"));
       for (uint32_t k = 0; k < R; k++)
         PSC_CUDA(cudaMemcpyAsync(B[k]->out, d + vbase[k], B[k]->n * 8, cudaMemcpyDefault, g->stream));
     } else {
       uint32_t* d;
       PSC_TRY(ensure_t(g, B_AUX0, n + 1, &d));
       PSC_TRY(cc_batch_run(g, S->cfg.cc_beta, d));
+      PSC_TRY(stamp("solve"));
       for (uint32_t k = 0; k < R; k++)
         PSC_CUDA(cudaMemcpyAsync(B[k]->out, d + vbase[k], B[k]->n * 4, cudaMemcpyDefault, g->stream));
     }
     return call_end(g);
   };
   const int st = body();
+  *launches = g->stats.kernel_launches;
   psc_graph_free(g);
+  if (tr) {
+    std::fprintf(stderr, "server batch kind %d requests %u n %llu m %llu:", kind, R,
+                 (unsigned long long)n, (unsigned long long)m);
+    for (auto& mk : marks) std::fprintf(stderr, " %s %.2f", mk.first, mk.second);
+    std::fprintf(stderr, " freed %.2f ms\n",
+                 std::chrono::duration<double, std::milli>(Clock::now() - t_begin).count());
+  }
   return st;
 }
 
 // Batch of the queue head's kind: requests in arrival order while they fit
-// the budget left (a lone request always fits an idle server).  Caller holds
-// the lock.  Returns false if nothing may start now.
+// the budget left and the batch's share of the budget (budget / workers, so
+// that a backlog is spread over all workers); a lone request always fits an
+// idle server.  Caller holds the lock.  Returns false if nothing may start.
 bool take_batch(psc_server_s* S, std::vector<Request*>& batch, int& kind, uint64_t& bytes) {
   if (S->queue.empty()) return false;
   const uint64_t budget = S->cfg.hbm_budget;
+  const uint64_t share = std::max<uint64_t>(1, budget / S->cfg.workers);
   kind = S->queue.front()->kind;
   bytes = 0;
   for (auto it = S->queue.begin(); it != S->queue.end() && batch.size() < S->cfg.max_batch;) {
@@ -165,8 +212,9 @@ bool take_batch(psc_server_s* S, std::vector<Request*>& batch, int& kind, uint64
       ++it;
       continue;
     }
-    const bool fits = S->used + bytes + r->bytes <= budget;
-    if (!fits && !(batch.empty() && S->running == 0)) break;
+    const bool fits = S->used + bytes + r->bytes <= budget && bytes + r->bytes <= share;
+    // a request larger than the share goes alone when the budget allows
+    if (!fits && !(batch.empty() && (S->running == 0 || S->used + r->bytes <= budget))) break;
     batch.push_back(r);
     bytes += r->bytes;
     it = S->queue.erase(it);
@@ -196,10 +244,12 @@ void worker_loop(psc_server_s* S) {
       r->t_start = t0;
       r->batch_size = (uint32_t)batch.size();
     }
-    const int st = run_batch(S, batch, kind);
+    uint64_t launches = 0;
+    const int st = run_batch(S, batch, kind, &launches);
     const auto t1 = Clock::now();
     {
       std::lock_guard<std::mutex> lk(S->mu);
+      S->stats.kernel_launches += launches;
       S->used -= bytes;
       S->running--;
       S->stats.busy_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
@@ -251,12 +301,14 @@ extern "C" int psc_server_create(const psc_server_config_t* cfg, psc_server_t* o
 }
 
 extern "C" int psc_server_submit(psc_server_t S, int kind, const uint64_t* off, const uint32_t* E,
-                                 uint64_t n, uint64_t m, uint64_t seed, void* labels_out,
-                                 uint64_t* id_out) {
+                                 const uint64_t* in_off, const uint32_t* in_E, uint64_t n,
+                                 uint64_t m, uint64_t seed, void* labels_out, uint64_t* id_out) {
   if (!S || !off || (m && !E) || !labels_out || !id_out || n == 0 || n >= 0xFFFFFFFFull)
     return PSC_ERR_INVALID;
   if (kind != PSC_REQ_SCC && kind != PSC_REQ_CC) return PSC_ERR_INVALID;
   if (off[0] != 0 || off[n] != m) return PSC_ERR_INVALID;
+  if ((in_off && m && !in_E) || (!in_off && in_E)) return PSC_ERR_INVALID;
+  if (in_off && (kind != PSC_REQ_SCC || in_off[0] != 0 || in_off[n] != m)) return PSC_ERR_INVALID;
   const uint64_t bytes = request_bytes(kind, n, m);
   auto* r = new Request();
   r->kind = kind;
@@ -264,6 +316,8 @@ extern "C" int psc_server_submit(psc_server_t S, int kind, const uint64_t* off, 
   r->m = m;
   r->off = off;
   r->E = E;
+  r->in_off = in_off;
+  r->in_E = in_E;
   r->seed = seed;
   r->out = labels_out;
   r->bytes = bytes;

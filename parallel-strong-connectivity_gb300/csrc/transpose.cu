@@ -154,7 +154,7 @@ __global__ void k_max_len(const uint64_t* __restrict__ in_off, uint64_t n, unsig
   if ((threadIdx.x & 31) == 0 && mx) atomicMax(out, mx);
 }
 
-int build_transpose(psc_graph_s* g) {
+int build_transpose(psc_graph_s* g, bool sorted) {
   const uint64_t n = g->n, m = g->m;
   uint32_t* cnt;
   PSC_TRY(ensure_t(g, B_TMP32, n + 1, &cnt));
@@ -175,6 +175,7 @@ int build_transpose(psc_graph_s* g) {
     k_scatter<256><<<grid_for(g, n, 256), 256, 0, g->stream>>>(g->off, g->E, n, g->in_off, cnt,
                                                                g->in_E);
   }
+  if (!sorted) return PSC_OK;
   // longest in-list decides the global scratch of the sort
   PSC_TRY(zero_counters(g));
   k_max_len<<<grid_for(g, n, 256), 256, 0, g->stream>>>(g->in_off, n, &g->ctr->aux0);

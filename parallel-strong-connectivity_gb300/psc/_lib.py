@@ -73,7 +73,8 @@ class ServerConfig(C.Structure):
 class ServerStats(C.Structure):
     """psc_server_stats_t (include/psc.h)."""
     _fields_ = [(f, C.c_uint64) for f in ("submitted", "completed", "failed", "rejected", "batches",
-                                          "peak_bytes", "max_running", "queued", "bytes_in_use")] + \
+                                          "peak_bytes", "max_running", "queued", "bytes_in_use",
+                                          "kernel_launches")] + \
         [("busy_ms", C.c_double)]
 
 
@@ -118,7 +119,7 @@ CUDA_SIGNATURES = {
     "psc_cc_batch": (I32, [P, D, P]),
     "psc_server_config_default": (None, [C.POINTER(ServerConfig)]),
     "psc_server_create": (I32, [C.POINTER(ServerConfig), C.POINTER(P)]),
-    "psc_server_submit": (I32, [P, I32, P, P, U64, U64, U64, P, C.POINTER(U64)]),
+    "psc_server_submit": (I32, [P, I32, P, P, P, P, U64, U64, U64, P, C.POINTER(U64)]),
     "psc_server_wait": (I32, [P, U64, C.POINTER(RequestInfo)]),
     "psc_server_drain": (I32, [P]),
     "psc_server_stats": (I32, [P, C.POINTER(ServerStats)]),

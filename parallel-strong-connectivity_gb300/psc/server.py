@@ -40,15 +40,25 @@ class Server:
         self.h = h.value
         self._live = {}  # id -> (arrays kept alive, labels)
 
-    def submit(self, g: HostGraph, kind: int = SCC, seed: int = 1) -> int:
+    def submit(self, g: HostGraph, kind: int = SCC, seed: int = 1,
+               with_transpose: bool = False) -> int:
+        """with_transpose: send g's host transpose along (SCC requests),
+        else the server builds it on the device."""
         off = np.ascontiguousarray(g.off, dtype=np.uint64)
         E = np.ascontiguousarray(g.E, dtype=np.uint32)
+        tin = (None, None)
+        if with_transpose and kind == SCC:
+            gt = g.with_transpose()
+            tin = (np.ascontiguousarray(gt.in_off, dtype=np.uint64),
+                   np.ascontiguousarray(gt.in_E, dtype=np.uint32))
         out = np.empty(g.n, np.uint64 if kind == SCC else np.uint32)
         rid = C.c_uint64()
-        check(self._lib.psc_server_submit(self.h, kind, off.ctypes.data,
-                                          E.ctypes.data if g.m else None, g.n, g.m, seed,
-                                          out.ctypes.data, C.byref(rid)), "psc_server_submit")
-        self._live[rid.value] = (off, E, out)
+        check(self._lib.psc_server_submit(
+            self.h, kind, off.ctypes.data, E.ctypes.data if g.m else None,
+            tin[0].ctypes.data if tin[0] is not None else None,
+            tin[1].ctypes.data if tin[1] is not None and g.m else None,
+            g.n, g.m, seed, out.ctypes.data, C.byref(rid)), "psc_server_submit")
+        self._live[rid.value] = (off, E, out, tin)
         return rid.value
 
     def wait(self, rid: int) -> tuple[np.ndarray, RequestInfo]:

@@ -44,7 +44,9 @@ def check_result(g, kind, seed, lab):
 def test_server_mixed_equals_solo():
     reqs = stream(40)
     with psc.Server(workers=3, max_batch=8) as srv:
-        ids = [srv.submit(g, kind, seed) for g, kind, seed in reqs]
+        # every other SCC request brings its host transpose
+        ids = [srv.submit(g, kind, seed, with_transpose=(k % 2 == 0))
+               for k, (g, kind, seed) in enumerate(reqs)]
         mixed = [srv.wait(i) for i in ids]
         st = srv.stats()
     assert st.completed == len(reqs) and st.failed == 0

@@ -156,6 +156,206 @@ __global__ void __launch_bounds__(BLOCK)
   }
 }
 
+// VGC round (the reference's sparse_update with its local queue,
+// ldd.hpp:88-161): each warp takes a chunk of up to `chunk` frontier
+// vertices (one while the frontier fits the grid, up to 32 when it is much
+// larger).  A chunk vertex with 0 < deg < tq seeds a local BFS in the warp's
+// shared-memory queue of tq = min(tau, kLddQueue) entries: each wave takes up
+// to 32 queued vertices, offers each one's label along its edges (balanced
+// expansion, kLddK edges per lane in flight, atomicCAS from NONE), keeps the
+// vertices it claims in the queue while there is room and spills the rest to
+// the next frontier, as is whatever is left when the queue fills.  Queued
+// vertices with deg > tq spill too; chunk vertices with deg >= tq go to the
+// `big` list, which the balanced push kernel expands afterwards.
+constexpr int kLddQueue = 512;
+constexpr int kLddVgcBlock = 128;
+constexpr int kLddK = 8;
+
+struct LEnt {
+  uint64_t beg;
+  uint32_t v;
+  uint32_t deg;
+};
+
+template <int BLOCK, int QCAP>
+__global__ void __launch_bounds__(BLOCK)
+    k_ldd_vgc(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
+              const uint32_t* __restrict__ qin, uint64_t nin, uint32_t* label, uint32_t* parent,
+              uint32_t* qout, uint32_t* big, uint32_t tau, uint32_t chunk, Counters* ctr) {
+  __shared__ WarpExpandSmem sm[BLOCK / 32];
+  __shared__ LEnt sq[BLOCK / 32][QCAP];
+  __shared__ uint32_t slab[BLOCK / 32][QCAP];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
+  uint32_t C = chunk < tq ? chunk : tq;
+  C = C < 1 ? 1 : C > 32 ? 32 : C;
+  LEnt* Q = sq[wid];
+  uint32_t* QL = slab[wid];
+  unsigned long long scanned = 0, next_edges = 0;
+  const uint64_t nchunks = (nin + C - 1) / C;
+  for (uint64_t c = gw; c < nchunks; c += nw) {
+    const uint64_t first = c * C;
+    const uint64_t left = nin - first;
+    const uint32_t cnt = left < C ? (uint32_t)left : C;
+    uint32_t u = 0, lu = 0;
+    uint64_t ub = 0, du = 0;
+    if (lane < cnt) {
+      u = qin[first + lane];
+      ub = off[u];
+      du = off[u + 1] - ub;
+      lu = label[u];
+    }
+    const bool isbig = lane < cnt && du >= tq;
+    {
+      const unsigned long long pos = warp_append(&ctr->heavy, isbig);
+      if (isbig) big[pos] = u;
+    }
+    const bool seed = lane < cnt && du > 0 && du < tq;
+    const uint32_t smask = __ballot_sync(kFull, seed);
+    if (seed) {
+      const uint32_t at = __popc(smask & ((1u << lane) - 1));
+      Q[at] = LEnt{ub, u, (uint32_t)du};
+      QL[at] = lu;
+    }
+    __syncwarp();
+    uint32_t head = 0, tail = __popc(smask);
+    while (head < tail && (head == 0 || tail < tq)) {
+      const uint32_t wave = min(32u, tail - head);
+      uint64_t beg = 0;
+      uint32_t deg = 0, x = 0, xl = 0, xdeg = 0;
+      bool spill_self = false;
+      if (lane < wave) {
+        const LEnt q = Q[head + lane];
+        x = q.v;
+        xl = QL[head + lane];
+        beg = q.beg;
+        deg = q.deg;
+        xdeg = q.deg;
+        if (deg > tq) {
+          spill_self = true;
+          deg = 0;
+        }
+      }
+      head += wave;
+      __syncwarp();
+      if (__any_sync(kFull, spill_self)) {
+        const unsigned long long pos = warp_append(&ctr->next, spill_self);
+        if (spill_self) {
+          qout[pos] = x;
+          next_edges += xdeg;
+        }
+      }
+      scanned += deg;
+      uint32_t incl = deg;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if ((int)lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      sm[wid].excl[lane] = incl - deg;
+      sm[wid].beg[lane] = beg;
+      __syncwarp();
+      for (uint32_t base = 0; base < total; base += 32 * kLddK) {
+        uint32_t w[kLddK], wl[kLddK], wp[kLddK];
+        uint64_t vb[kLddK], ve[kLddK];
+#pragma unroll
+        for (int k = 0; k < kLddK; k++) {
+          const uint32_t gi = base + k * 32 + lane;
+          w[k] = kNone;
+          wl[k] = 0;
+          wp[k] = 0;
+          if (gi < total) {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (sm[wid].excl[mid] <= gi)
+                lo = mid;
+              else
+                hi = mid - 1;
+            }
+            w[k] = __ldg(&E[sm[wid].beg[lo] + (gi - sm[wid].excl[lo])]);
+            wl[k] = QL[head - wave + lo];
+            wp[k] = Q[head - wave + lo].v;
+          }
+        }
+        // claims: the adjacency range is loaded alongside (used if claimed)
+        uint32_t tm = 0;
+#pragma unroll
+        for (int k = 0; k < kLddK; k++) {
+          vb[k] = ve[k] = 0;
+          if (w[k] != kNone && __ldcg(&label[w[k]]) == kNone) {
+            vb[k] = __ldg(&off[w[k]]);
+            ve[k] = __ldg(&off[w[k] + 1]);
+            tm |= 1u << k;
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kLddK; k++)
+          if (tm & (1u << k)) {
+            if (atomicCAS(&label[w[k]], kNone, wl[k]) == kNone) {
+              if (parent) parent[w[k]] = wp[k];
+            } else {
+              tm &= ~(1u << k);
+            }
+          }
+        // place: into the queue while it has room, then spill
+        const uint32_t cntk = __popc(tm);
+        uint32_t inc = cntk;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(kFull, inc, o);
+          if ((int)lane >= o) inc += t;
+        }
+        const uint32_t tot = __shfl_sync(kFull, inc, 31);
+        if (tot) {
+          const uint32_t room = tail < tq ? tq - tail : 0;
+          const uint32_t nloc = tot < room ? tot : room;
+          unsigned long long sbase = 0;
+          if (tot > nloc && lane == 0) sbase = atomicAdd(&ctr->next, (unsigned long long)(tot - nloc));
+          sbase = __shfl_sync(kFull, sbase, 0);
+          uint32_t r = inc - cntk;
+#pragma unroll
+          for (int k = 0; k < kLddK; k++)
+            if (tm & (1u << k)) {
+              const uint64_t vd = ve[k] - vb[k];
+              if (r < nloc) {
+                Q[tail + r] = LEnt{vb[k], w[k], (uint32_t)(vd < 0xFFFFFFFFull ? vd : 0xFFFFFFFFull)};
+                QL[tail + r] = wl[k];
+              } else {
+                qout[sbase + (r - nloc)] = w[k];
+                next_edges += vd;
+              }
+              r++;
+            }
+          tail += nloc;
+          __syncwarp();
+        }
+      }
+    }
+    // spill what is left in the queue with one reservation
+    const uint32_t rem = tail - head;
+    if (rem) {
+      unsigned long long b0 = 0;
+      if (lane == 0) b0 = atomicAdd(&ctr->next, (unsigned long long)rem);
+      b0 = __shfl_sync(kFull, b0, 0);
+      for (uint32_t k = lane; k < rem; k += 32) {
+        qout[b0 + k] = Q[head + k].v;
+        next_edges += Q[head + k].deg;
+      }
+    }
+    __syncwarp();
+  }
+  scanned = warp_sum(scanned);
+  next_edges = warp_sum(next_edges);
+  if (lane == 0) {
+    if (scanned) atomicAdd(&ctr->edges, scanned);
+    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
+  }
+}
+
 // Pull round (ldd.hpp:163-247): every unlabelled vertex takes the label of
 // its first neighbour in the frontier bitmap.  A warp owns 32 consecutive
 // vertices and writes their next-frontier word with one store.
@@ -404,9 +604,35 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
     }
     PSC_TRY(zero_counters(g));
     if (!pull) {
-      ProfScope ps(g, F_CC);
-      k_ldd_push<kCcBlock, 4><<<grid_for(g, nf, tb), tb, 0, g->stream>>>(
-          g->off, g->E, qa, nf, d_label, tree, qb, g->ctr);
+      // VGC round on a resident grid, then the big-degree frontier vertices
+      // it set aside, expanded by the balanced push kernel into the same queue
+      if (!g->ldd_vgc_blocks) {
+        PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &g->ldd_vgc_blocks, k_ldd_vgc<kLddVgcBlock, kLddQueue>, kLddVgcBlock, 0));
+        if (g->ldd_vgc_blocks < 1) g->ldd_vgc_blocks = 1;
+      }
+      const uint64_t max_blocks = (uint64_t)g->num_sms * g->ldd_vgc_blocks;
+      const uint64_t max_warps = max_blocks * (kLddVgcBlock / 32);
+      const uint64_t chunk = std::min<uint64_t>(32, (nf + max_warps - 1) / max_warps);
+      const uint64_t chunks = (nf + chunk - 1) / chunk;
+      const uint64_t blocks =
+          std::min(max_blocks, (chunks + kLddVgcBlock / 32 - 1) / (kLddVgcBlock / 32));
+      uint32_t* big;
+      PSC_TRY(ensure_t(g, B_HEAVY, n + 1, &big));
+      {
+        ProfScope ps(g, F_CC);
+        k_ldd_vgc<kLddVgcBlock, kLddQueue>
+            <<<(unsigned)std::max<uint64_t>(1, blocks), kLddVgcBlock, 0, g->stream>>>(
+                g->off, g->E, qa, nf, d_label, tree, qb, big, kLddQueue, (uint32_t)chunk, g->ctr);
+      }
+      PSC_CUDA(cudaGetLastError());
+      PSC_TRY(read_counters(g));
+      const uint64_t nbig = g->hctr[0].heavy;
+      if (nbig) {
+        ProfScope ps(g, F_CC);
+        k_ldd_push<kCcBlock, 4><<<grid_for(g, nbig, tb), tb, 0, g->stream>>>(
+            g->off, g->E, big, nbig, d_label, tree, qb, g->ctr);
+      }
       std::swap(qa, qb);
       swap_bufs(g, B_QA, B_QB);
     } else {
@@ -465,12 +691,12 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
     k_ldd_tree_edges<<<grid_for(g, n, 256), 256, 0, g->stream>>>(tree, n, forest, g->ctr);
   }
   {
-    ProfScope ps(g, F_CC);
+    ProfScope ps(g, F_UF);
     k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(g->off, g->E, n, d_label,
                                                                    max_label, forest, g->ctr);
   }
   {
-    ProfScope ps(g, F_CC);
+    ProfScope ps(g, F_UF);
     k_uf_final<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, n);
   }
   PSC_CUDA(cudaGetLastError());

@@ -45,6 +45,7 @@ enum Family : int {
   F_LE,
   F_TRANSPOSE,
   F_BATCH,
+  F_UF,
   F_COUNT
 };
 extern const char* const kFamilyName[F_COUNT];
@@ -104,6 +105,7 @@ struct psc_graph_s {
   int num_sms = 0;
   int vgc_blocks = 0;     // resident blocks per SM of the reach VGC kernel
   int ms_vgc_blocks = 0;  // same for the multi-search VGC kernel
+  int ldd_vgc_blocks = 0; // same for the LDD VGC kernel
   // named scratch buffers, grown on demand (stream-ordered allocator)
   std::vector<psc::DevBuf> bufs;
   psc::Counters* ctr = nullptr;   // device, kCounterSets blocks

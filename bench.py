@@ -281,6 +281,17 @@ def run_ncu_step(args) -> None:
     and one solve, and nothing else (no CPU baseline, no end-to-end pass)."""
     import psc
 
+    if args.workload == "batch":
+        g, vb = psc.batch_workload(args.batch_count, **BATCH)
+        seeds = (BATCH["seed0"] + np.arange(args.batch_count)).astype(np.uint64)
+        with psc.DeviceGraph(g) as dg:
+            dg.set_batch(vb)
+            for _ in range(2):
+                dg.scc_batch(psc.default_params(), seeds)
+            st = dg.stats()
+            log(f"ncu step: batch of {args.batch_count} n={g.n} m={g.m} {st.total_ms:.2f} ms, "
+                f"{st.kernel_launches} launches")
+        return
     wl = WORKLOADS[args.workload]
     g = wl["make"](psc)
     with psc.DeviceGraph(g) as dg:
@@ -678,7 +689,12 @@ def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
                       "restatement of src/scc.hpp)"}
 
 
-def roofline_of(prof: dict, steps: int) -> dict:
+# DRAM bytes (read + write) of one launch of a workload's dominant kernel from
+# one ncu capture of the same command (profiles/k_reach_vgc_knn1e7.md).
+NCU_TRAFFIC = {("scc_knn", "reach_vgc"): 103.0e6}
+
+
+def roofline_of(prof: dict, steps: int, workload: str = "") -> dict:
     fam, top = max(prof.items(), key=lambda kv: kv[1]["ms"])
     peak, peak_kind = peaks()
     achieved = (top["bytes"] / top["launches"]) / (top["ms"] / top["launches"] / 1e3) / 1e9 \
@@ -686,7 +702,8 @@ def roofline_of(prof: dict, steps: int) -> dict:
     prof_total = sum(v["ms"] for v in prof.values())
     return {
         "bound": "hbm", "kernel": fam, "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+        "frac": achieved / peak, "peak_source": peak_kind,
+        "traffic": NCU_TRAFFIC.get((workload, fam)),
         "launches": top["launches"] // max(1, steps),
         "share": top["ms"] / prof_total if prof_total else None,
         "bytes_per_launch": top["bytes"] / max(1, top["launches"]),
@@ -752,7 +769,7 @@ def run_gpu(args, world, rank, local, dist) -> None:
         dg.scc_device(d_labels.value, params)
     prof = dg.profile()
     dg.set_profiling(False)
-    roofline = roofline_of(prof, args.profile_steps)
+    roofline = roofline_of(prof, args.profile_steps, f"scc_{args.workload}")
 
     # end to end through the C ABI with pinned host buffers
     h2d = h_off.nbytes + h_E.nbytes + h_in_off.nbytes + h_in_E.nbytes

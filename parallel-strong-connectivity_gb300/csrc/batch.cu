@@ -53,25 +53,54 @@ __global__ void k_fill_gid(const uint64_t* __restrict__ vbase, uint32_t G, uint6
     gid[v] = last_le(vbase, G + 1, v);
 }
 
-// Every edge of both directions stays inside its graph's id range.
-__global__ void k_check_batch(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
-                              const uint64_t* __restrict__ in_off, const uint32_t* __restrict__ in_E,
-                              const uint64_t* __restrict__ vbase, const uint32_t* __restrict__ gid,
-                              uint64_t n, unsigned long long* bad) {
-  const unsigned lane = lane_id();
-  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  uint32_t found = 0;
-  for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
-    const uint32_t k = gid[u];
-    const uint64_t lo = vbase[k], hi = vbase[k + 1];
+// Every edge of both directions stays inside its graph's id range: 32
+// vertices per warp step, their edges checked by a balanced warp expansion.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    k_check_batch(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
+                  const uint64_t* __restrict__ in_off, const uint32_t* __restrict__ in_E,
+                  const uint64_t* __restrict__ vbase, const uint32_t* __restrict__ gid, uint64_t n,
+                  unsigned long long* bad) {
+  __shared__ WarpExpandSmem sm[BLOCK / 32];
+  __shared__ uint32_t s_lo[BLOCK], s_hi[BLOCK];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  bool found = false;
+  for (uint64_t base = gw * 32; base < n; base += nw * 32) {
+    const uint64_t u = base + lane;
+    uint32_t lo = 0, hi = 0;
+    if (u < n) {
+      const uint32_t k = gid[u];
+      lo = (uint32_t)vbase[k];
+      hi = (uint32_t)vbase[k + 1];
+    }
+    s_lo[wid * 32 + lane] = lo;
+    s_hi[wid * 32 + lane] = hi;
+    __syncwarp();
+#pragma unroll 1
     for (int d = 0; d < 2; d++) {
       const uint64_t* O = d ? in_off : off;
       const uint32_t* A = d ? in_E : E;
-      for (uint64_t e = O[u] + lane; e < O[u + 1]; e += 32) {
-        const uint32_t v = A[e];
-        found |= (v < lo || v >= hi) ? 1u : 0u;
+      uint64_t beg = 0, rem = 0;
+      if (u < n) {
+        beg = O[u];
+        rem = O[u + 1] - beg;
+      }
+      // lists in pieces of at most 2^26 edges (32-bit warp scan)
+      while (__any_sync(kFull, rem > 0)) {
+        const uint32_t piece = (uint32_t)(rem < (1ull << 26) ? rem : (1ull << 26));
+        warp_expand(sm[wid], beg, piece, [&](bool act, int src, uint64_t e) {
+          if (act) {
+            const uint32_t v = __ldg(&A[e]);
+            found |= v < s_lo[wid * 32 + src] || v >= s_hi[wid * 32 + src];
+          }
+        });
+        beg += piece;
+        rem -= piece;
       }
     }
+    __syncwarp();
   }
   if (__any_sync(kFull, found) && lane == 0) atomicAdd(bad, 1ull);
 }
@@ -483,7 +512,7 @@ int batch_attach(psc_graph_s* g, const uint64_t* vbase, uint32_t num_graphs, boo
   PSC_CUDA(cudaGetLastError());
   if (check) {
     PSC_CUDA(cudaMemsetAsync(&g->ctr->aux0, 0, 8, g->stream));
-    k_check_batch<<<grid_for(g, g->n * 32, 256), 256, 0, g->stream>>>(
+    k_check_batch<256><<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(
         g->off, g->E, g->in_off, g->in_E, g->d_vbase, g->d_gid, g->n, &g->ctr->aux0);
     PSC_CUDA(cudaGetLastError());
     PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux0, &g->ctr->aux0, 8, cudaMemcpyDeviceToHost, g->stream));

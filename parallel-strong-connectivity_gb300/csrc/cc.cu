@@ -469,7 +469,8 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t* p, uint32_t x) {
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_uf_edges(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E, uint64_t n,
-               uint32_t* parent, uint32_t max_root, uint32_t* forest, Counters* ctr) {
+               uint32_t* parent, const uint32_t* __restrict__ cluster, uint32_t max_root,
+               uint32_t* forest, Counters* ctr) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ uint32_t s_u[BLOCK];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -491,9 +492,14 @@ __global__ void __launch_bounds__(BLOCK)
       warp_expand(sm[wid], beg, piece, [&](bool act, int s, uint64_t e) {
         bool linked = false;
         uint32_t x = 0, y = 0;
+        // an edge inside one LDD cluster joins nothing (both ends already
+        // share the cluster's centre as an ancestor)
         if (act) {
           x = s_u[wid * 32 + s];
           y = __ldg(&E[e]);
+          if (__ldg(&cluster[y]) == __ldg(&cluster[x])) act = false;
+        }
+        if (act) {
           for (;;) {
             uint32_t rx = uf_find(parent, x), ry = uf_find(parent, y);
             if (rx == ry) break;
@@ -690,10 +696,14 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
     ProfScope ps(g, F_CC);
     k_ldd_tree_edges<<<grid_for(g, n, 256), 256, 0, g->stream>>>(tree, n, forest, g->ctr);
   }
+  // the LDD clusters, kept unchanged while the unions rewrite d_label
+  uint32_t* cluster;
+  PSC_TRY(ensure_t(g, B_AUX1, n + 1, &cluster));
+  PSC_CUDA(cudaMemcpyAsync(cluster, d_label, n * 4, cudaMemcpyDeviceToDevice, g->stream));
   {
     ProfScope ps(g, F_UF);
-    k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(g->off, g->E, n, d_label,
-                                                                   max_label, forest, g->ctr);
+    k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(
+        g->off, g->E, n, d_label, cluster, max_label, forest, g->ctr);
   }
   {
     ProfScope ps(g, F_UF);

@@ -331,6 +331,7 @@ def run_batch(args, world, rank, local, dist) -> None:
     n, m = g.n, g.m
     seeds = (BATCH["seed0"] + np.arange(count)).astype(np.uint64)
     params = psc.default_params()
+    tune = None
 
     pin = Pinned(lib)
     h_off, h_E = pin.copy(g.off), pin.copy(g.E)
@@ -341,6 +342,14 @@ def run_batch(args, world, rank, local, dist) -> None:
     dg.set_batch(vb)
     d_labels = C.c_void_p()
     _lib.check(lib.psc_device_alloc(n * 8, C.byref(d_labels)), "psc_device_alloc")
+    if not args.no_tune:
+        # the autotuner picks tau / pull threshold / block / beta on this
+        # batch before the timed region; every comparison below uses them
+        params, rep = dg.tune(params, seeds, reps=1)
+        tune = {"tau": params.tau, "pull_div": params.pull_div, "block": params.block,
+                "beta": params.beta, "start_ms": rep.start_ms, "best_ms": rep.best_ms,
+                "trials": rep.trials}
+        log(f"[rank {rank}] tuned: {tune}")
     for _ in range(args.warmup):
         dg.scc_batch_device(d_labels.value, params, seeds)
     ref_labels = dg.scc_batch(params, seeds)
@@ -381,7 +390,8 @@ def run_batch(args, world, rank, local, dist) -> None:
     mismatched = 0
     for k in sample:
         mk = g.member(vb, k)
-        pk = psc.default_params(seed=int(seeds[k]))
+        pk = psc.default_params(seed=int(seeds[k]), tau=params.tau, pull_div=params.pull_div,
+                                block=params.block, beta=params.beta)
         with psc.DeviceGraph(mk) as d1:
             lab1 = d1.scc(pk)  # warm-up and check
             if not np.array_equal(lab1, ref_labels[int(vb[k]):int(vb[k + 1])]):
@@ -442,7 +452,9 @@ def run_batch(args, world, rank, local, dist) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic",
         "config": {"workload": f"scc_batch{count}", "graph": batch_desc(count), "graphs": count,
-                   "n": n, "m": m, "beta": 1.5, "tau": 512, "vgc": True,
+                   "n": n, "m": m, "beta": params.beta, "tau": params.tau,
+                   "pull_div": params.pull_div, "block": params.block, "vgc": True,
+                   "autotune": tune,
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)",
                    "edges_per_s": m * args.steps * world / (total_ms / 1e3),
                    "batches": last.batches, "subrounds": last.subrounds,
@@ -839,6 +851,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=SERVE["requests"],
                     help="requests per arrival rate of the serve workload")
     ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--no-tune", action="store_true",
+                    help="batch workload: keep the default parameters")
     ap.add_argument("--batch-count", type=int, default=4096,
                     help="graphs in the batch workload")
     ap.add_argument("--plain-sample", type=int, default=256,

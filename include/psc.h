@@ -47,7 +47,7 @@ typedef struct {
   int32_t local_scc;   /* -local_scc: VGC in the multi-search */
   uint64_t seed;       /* pivot permutation seed (stands in for parlay::random_shuffle) */
   /* tuning knobs (0 = library default) */
-  uint32_t block;      /* threads per block of the expansion kernels */
+  uint32_t block;      /* threads per block of the push / pull / expansion kernels: 128, 256 or 512 (256) */
   uint32_t pull_div;   /* reach switches to pull when frontier edges > m / pull_div (20) */
 } psc_params_t;
 
@@ -141,6 +141,22 @@ int psc_scc_batch_device(psc_graph_t g, const psc_params_t* p, const uint64_t* s
  * u32[n], each vertex's component root as a vertex id local to its graph (the
  * same partition as psc_cc on each graph alone). */
 int psc_cc_batch(psc_graph_t g, double beta, uint32_t* labels_out);
+
+/* Autotuner of the SCC parameters on this graph (or batch, with per-graph
+ * seeds as psc_scc_batch; seeds is ignored for a plain graph).  No
+ * counterpart in the reference.  Coordinate descent from *p over tau
+ * {32, 64, 128, 256, 512}, pull_div {5, 10, 20, 40, 80}, block
+ * {128, 256, 512} and beta {1.5, 2, 3, 4}; each candidate solve is timed
+ * `reps` times (0: 2) and must be 2 % faster to be kept.  *p receives the
+ * best parameters.  tau, pull_div and block never change the labels; beta
+ * changes label values, never the partition. */
+typedef struct {
+  double start_ms;  /* solve time with the starting parameters */
+  double best_ms;   /* solve time with the returned parameters */
+  uint32_t trials;  /* parameter settings timed */
+} psc_tune_report_t;
+int psc_tune_scc(psc_graph_t g, const uint64_t* seeds, uint32_t reps, psc_params_t* p,
+                 psc_tune_report_t* report);
 
 /* Request server: SCC and connectivity solves of independent graphs served
  * with continuous batching under a device-memory budget.  No counterpart in

@@ -483,7 +483,10 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
 }
 
 int scc_batch_run(psc_graph_s* g, const psc_params_t* p, const uint64_t* seeds, uint64_t* labels) {
-  return scc_timed(g, [&](psc_graph_s* h) { return scc_batch_phases(h, labels, p, seeds); });
+  g->block = p->block;
+  const int st = scc_timed(g, [&](psc_graph_s* h) { return scc_batch_phases(h, labels, p, seeds); });
+  g->block = 0;
+  return st;
 }
 
 }  // namespace psc

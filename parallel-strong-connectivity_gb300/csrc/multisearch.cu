@@ -256,7 +256,7 @@ __device__ __forceinline__ void flush_ms_counters(Counters* c0, Counters* c1,
 
 // Expansion sub-round for up to two sides: 32 pairs per warp step.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 3)
+__global__ void __launch_bounds__(BLOCK, (768 / BLOCK) > 0 ? (768 / BLOCK) : 1)
     k_ms_expand(MsSide s0, MsSide s1, const uint64_t* __restrict__ labels) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ MsSrc ssrc[BLOCK / 32];
@@ -788,8 +788,17 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
     }
     if (ne) {
       ProfScope ps(g, F_MS_EXPAND);
-      k_ms_expand<kMsBlock><<<grid_for(g, e_items, kMsBlock), kMsBlock, 0, g->stream>>>(ex[0], ex[1],
-                                                                                        labels);
+      switch (p->block) {
+        case 128:
+          k_ms_expand<128><<<grid_for(g, e_items, 128), 128, 0, g->stream>>>(ex[0], ex[1], labels);
+          break;
+        case 512:
+          k_ms_expand<512><<<grid_for(g, e_items, 512), 512, 0, g->stream>>>(ex[0], ex[1], labels);
+          break;
+        default:
+          k_ms_expand<kMsBlock><<<grid_for(g, e_items, kMsBlock), kMsBlock, 0, g->stream>>>(
+              ex[0], ex[1], labels);
+      }
     }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(read_counters(g));

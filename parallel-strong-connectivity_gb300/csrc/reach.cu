@@ -727,17 +727,41 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
     }
     if (np) {
       ProfScope ps(g, F_REACH_PUSH);
-      k_reach_push<kReachBlock><<<grid_for(g, p_items, kReachBlock), kReachBlock, 0, g->stream>>>(
-          pu[0], pu[1]);
+      switch (g->block) {
+        case 128:
+          k_reach_push<128><<<grid_for(g, p_items, 128), 128, 0, g->stream>>>(pu[0], pu[1]);
+          break;
+        case 512:
+          k_reach_push<512><<<grid_for(g, p_items, 512), 512, 0, g->stream>>>(pu[0], pu[1]);
+          break;
+        default:
+          k_reach_push<kReachBlock><<<grid_for(g, p_items, kReachBlock), kReachBlock, 0,
+                                      g->stream>>>(pu[0], pu[1]);
+      }
     }
     for (int k = 0; k < ns; k++) {
       if (mode[k] != M_PULL) continue;
       Side& s = sides[k];
       ProfScope ps(g, F_REACH_PULL);
-      k_reach_pull<kReachBlock><<<grid_for(g, nwords * 32, kReachBlock), kReachBlock, 0, g->stream>>>(
-          s.backward ? g->off : g->in_off, s.backward ? g->E : g->in_E,
-          s.backward ? g->in_off : g->off, (const uint32_t*)g->bufs[s.slot_fa].p, s.vis,
-          (uint32_t*)g->bufs[s.slot_fb].p, n, g->ctr + s.cset);
+      const uint64_t* B_off = s.backward ? g->off : g->in_off;
+      const uint32_t* B_E = s.backward ? g->E : g->in_E;
+      const uint64_t* A_off = s.backward ? g->in_off : g->off;
+      const uint32_t* fa = (const uint32_t*)g->bufs[s.slot_fa].p;
+      uint32_t* fbo = (uint32_t*)g->bufs[s.slot_fb].p;
+      switch (g->block) {
+        case 128:
+          k_reach_pull<128><<<grid_for(g, nwords * 32, 128), 128, 0, g->stream>>>(
+              B_off, B_E, A_off, fa, s.vis, fbo, n, g->ctr + s.cset);
+          break;
+        case 512:
+          k_reach_pull<512><<<grid_for(g, nwords * 32, 512), 512, 0, g->stream>>>(
+              B_off, B_E, A_off, fa, s.vis, fbo, n, g->ctr + s.cset);
+          break;
+        default:
+          k_reach_pull<kReachBlock><<<grid_for(g, nwords * 32, kReachBlock), kReachBlock, 0,
+                                      g->stream>>>(B_off, B_E, A_off, fa, s.vis, fbo, n,
+                                                   g->ctr + s.cset);
+      }
     }
     PSC_CUDA(cudaGetLastError());
     cudaEvent_t tr_b = nullptr;

@@ -125,7 +125,10 @@ int scc_phase_times(psc_graph_s* g) {
 }
 
 int scc_run(psc_graph_s* g, const psc_params_t* p, uint64_t* labels) {
-  return scc_timed(g, [&](psc_graph_s* h) { return scc_phases(h, labels, p); });
+  g->block = p->block;
+  const int st = scc_timed(g, [&](psc_graph_s* h) { return scc_phases(h, labels, p); });
+  g->block = 0;
+  return st;
 }
 
 int scc_partition(psc_graph_s* g, const MsResult res[2], uint64_t* labels) {

@@ -88,6 +88,11 @@ class RequestInfo(C.Structure):
     ]
 
 
+class TuneReport(C.Structure):
+    """psc_tune_report_t (include/psc.h)."""
+    _fields_ = [("start_ms", C.c_double), ("best_ms", C.c_double), ("trials", C.c_uint32)]
+
+
 P = C.c_void_p
 U64 = C.c_uint64
 U32 = C.c_uint32
@@ -117,6 +122,7 @@ CUDA_SIGNATURES = {
     "psc_scc_batch": (I32, [P, C.POINTER(Params), P, P]),
     "psc_scc_batch_device": (I32, [P, C.POINTER(Params), P, P]),
     "psc_cc_batch": (I32, [P, D, P]),
+    "psc_tune_scc": (I32, [P, P, U32, C.POINTER(Params), C.POINTER(TuneReport)]),
     "psc_server_config_default": (None, [C.POINTER(ServerConfig)]),
     "psc_server_create": (I32, [C.POINTER(ServerConfig), C.POINTER(P)]),
     "psc_server_submit": (I32, [P, I32, P, P, P, P, U64, U64, U64, P, C.POINTER(U64)]),

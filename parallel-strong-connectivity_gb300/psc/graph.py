@@ -305,6 +305,17 @@ class DeviceGraph:
         check(self._lib.psc_scc_batch_device(self.h, C.byref(p), _ptr(sd), d_labels),
               "psc_scc_batch_device")
 
+    def tune(self, params: Params | None = None, seeds=None, reps: int = 2):
+        """Autotuned SCC parameters for this graph or batch: (params, report)."""
+        p = params or default_params()
+        q = Params()
+        C.memmove(C.byref(q), C.byref(p), C.sizeof(Params))
+        sd = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.uint64)
+        rep = _lib.TuneReport()
+        check(self._lib.psc_tune_scc(self.h, _ptr(sd), reps, C.byref(q), C.byref(rep)),
+              "psc_tune_scc")
+        return q, rep
+
     def cc_batch(self, beta: float = 0.2) -> np.ndarray:
         """Connectivity roots of every graph of a symmetric batch, local ids."""
         labels = np.empty(self.n, np.uint32)

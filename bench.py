@@ -157,20 +157,26 @@ class Pinned:
         self.ptrs = []
 
 
-def cpu_baseline(g, workload: str, budget_s: float = 15.0, max_runs: int = 20) -> dict:
+def cpu_baseline(g, workload: str, gpu_labels=None, budget_s: float = 15.0,
+                 max_runs: int = 20) -> dict:
+    """The oracle timed on the host cores; its labels of the first run are
+    compared with the GPU's (raw u64 labels, same seed)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
 
     threads = os.cpu_count() or 1
-    runs, t_total = 0, 0.0
+    runs, t_total, same = 0, 0.0, None
     while runs < max_runs and (runs == 0 or t_total < budget_s):
         t = time.perf_counter()
-        pyoracle.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=1, nthreads=threads)
+        lab = pyoracle.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=1, nthreads=threads)
         t_total += time.perf_counter() - t
+        if runs == 0 and gpu_labels is not None:
+            same = bool(np.array_equal(lab, gpu_labels))
         runs += 1
     return {"value": g.m * runs / t_total, "unit": "edges/s", "cores": threads, "kind": "port",
             "sample": f"{runs} full SCC solve(s) of the {workload} workload, "
-                      f"{t_total / runs * 1e3:.1f} ms each (OpenMP restatement of src/scc.hpp)"}
+                      f"{t_total / runs * 1e3:.1f} ms each (OpenMP restatement of src/scc.hpp)",
+            "labels_equal_gpu": same}
 
 
 def dist_setup():
@@ -809,11 +815,14 @@ def run_gpu(args, world, rank, local, dist) -> None:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(g, args.workload)
+        cpu = cpu_baseline(g, args.workload, ref_labels)
+        if cpu["labels_equal_gpu"] is False:
+            raise SystemExit("GPU labels differ from the oracle's")
 
     lib.psc_device_free(d_labels.value)
     dg.free()
     pin.free()
+    extra = cc_le_extra(psc, g, rank, world, args) if args.workload == "rmat26" else {}
     if rank != 0:
         return
     line = {
@@ -838,7 +847,37 @@ def run_gpu(args, world, rank, local, dist) -> None:
         "clocks": clocks,
         "gpu_launches": launches,
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
+
+
+def cc_le_extra(psc, g, rank, world, args) -> dict:
+    """The rest of the R-MAT 2^26 configuration: connectivity and LE-lists
+    (permutation seed 4) on the symmetrised graph, resident on the device,
+    with the oracle's connectivity timed beside it (rank 0)."""
+    t = time.perf_counter()
+    s = g.symmetrize()
+    log(f"[rank {rank}] symmetrised: m = {s.m} in {time.perf_counter() - t:.1f}s")
+    out = {}
+    with psc.DeviceGraph(s) as dg:
+        lab = dg.cc()
+        cc_ms = min((dg.cc(), dg.stats().total_ms)[1] for _ in range(3))
+        perm = psc.random_permutation(s.n, 4)
+        le = dg.lelist(perm)
+        le_ms = dg.stats().total_ms
+    out["connectivity"] = {"ms": cc_ms, "edges_per_s": s.m / (cc_ms / 1e3), "m_sym": s.m,
+                           "components": int(len(np.unique(lab)))}
+    out["lelist"] = {"ms": le_ms, "triples": int(len(le)), "perm_seed": 4}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+        t = time.perf_counter()
+        ref = pyoracle.cc(s.n, s.off, s.E, nthreads=os.cpu_count() or 1)
+        cpu_ms = (time.perf_counter() - t) * 1e3
+        out["connectivity"]["cpu_ms"] = cpu_ms
+        out["connectivity"]["partition_equal_oracle"] = bool(
+            np.array_equal(pyoracle.canon(ref), pyoracle.canon(lab)))
+    return out
 
 
 def main():

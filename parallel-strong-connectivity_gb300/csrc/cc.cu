@@ -463,14 +463,15 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t* p, uint32_t x) {
   return x;
 }
 
-// Unite over the edges of every vertex whose root is not the largest
-// cluster's (Connectivity.h:74-93).  Link the larger root under the smaller
-// (UniteRemCAS links high -> low, union_find_rules.h:193-225).
+// Unite over the edges [first, last) of the adjacency list of every vertex
+// whose root is not max_root (Connectivity.h:74-93).  Link the larger root
+// under the smaller (UniteRemCAS links high -> low,
+// union_find_rules.h:193-225).
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_uf_edges(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E, uint64_t n,
                uint32_t* parent, const uint32_t* __restrict__ cluster, uint32_t max_root,
-               uint32_t* forest, Counters* ctr) {
+               uint32_t first, uint32_t last, uint32_t* forest, Counters* ctr) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ uint32_t s_u[BLOCK];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -481,8 +482,10 @@ __global__ void __launch_bounds__(BLOCK)
     const uint64_t i = base + lane;
     uint64_t beg = 0, rem = 0;
     if (i < n && uf_find(parent, (uint32_t)i) != max_root) {
-      beg = off[i];
-      rem = off[i + 1] - beg;
+      const uint64_t b = off[i], d = off[i + 1] - b;
+      const uint64_t lo = d < first ? d : first, hi = d < last ? d : last;
+      beg = b + lo;
+      rem = hi - lo;
     }
     scanned += rem;
     s_u[wid * 32 + lane] = (uint32_t)i;
@@ -700,10 +703,32 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
   uint32_t* cluster;
   PSC_TRY(ensure_t(g, B_AUX1, n + 1, &cluster));
   PSC_CUDA(cudaMemcpyAsync(cluster, d_label, n * 4, cudaMemcpyDeviceToDevice, g->stream));
+  // Two passes over the edges of vertices outside the largest component:
+  // first each one's first kUfSample edges (adjacency lists are sorted, so
+  // these reach low-id hubs, which join most vertices to the largest
+  // component), then, after compressing, the rest of the edges of the
+  // vertices still outside it.  Every edge is still offered to the union
+  // from one side: an edge skipped on both sides joins two vertices already
+  // in the largest component.
+  constexpr uint32_t kUfSample = 2;
   {
     ProfScope ps(g, F_UF);
     k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(
-        g->off, g->E, n, d_label, cluster, max_label, forest, g->ctr);
+        g->off, g->E, n, d_label, cluster, max_label, 0, kUfSample, forest, g->ctr);
+  }
+  {
+    ProfScope ps(g, F_UF);
+    k_uf_final<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, n);
+  }
+  PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux1, d_label + max_label, 4, cudaMemcpyDeviceToHost,
+                           g->stream));
+  PSC_CUDA(cudaStreamSynchronize(g->stream));
+  uint32_t max_root = 0;
+  std::memcpy(&max_root, &g->hctr->aux1, 4);
+  {
+    ProfScope ps(g, F_UF);
+    k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(
+        g->off, g->E, n, d_label, cluster, max_root, kUfSample, 0xFFFFFFFFu, forest, g->ctr);
   }
   {
     ProfScope ps(g, F_UF);

@@ -471,6 +471,7 @@ template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_uf_edges(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E, uint64_t n,
                uint32_t* parent, const uint32_t* __restrict__ cluster, uint32_t max_root,
+               const uint32_t* __restrict__ gid, const uint32_t* __restrict__ groot,
                uint32_t first, uint32_t last, uint32_t* forest, Counters* ctr) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ uint32_t s_u[BLOCK];
@@ -481,7 +482,7 @@ __global__ void __launch_bounds__(BLOCK)
   for (uint64_t base = gw * 32; base < n; base += nw * 32) {
     const uint64_t i = base + lane;
     uint64_t beg = 0, rem = 0;
-    if (i < n && uf_find(parent, (uint32_t)i) != max_root) {
+    if (i < n && uf_find(parent, (uint32_t)i) != (gid ? groot[gid[i]] : max_root)) {
       const uint64_t b = off[i], d = off[i + 1] - b;
       const uint64_t lo = d < first ? d : first, hi = d < last ? d : last;
       beg = b + lo;
@@ -540,6 +541,56 @@ __global__ void k_uf_final(uint32_t* parent, uint64_t n) {
     parent[i] = uf_find(parent, (uint32_t)i);
 }
 
+// Most frequent LDD label among kGraphSamples hashed samples of each graph of
+// a batch (ties to the smallest label, as the single-graph scan of sorted
+// samples): one block per graph, a bitonic sort in shared memory.
+constexpr int kGraphSamples = 256;
+
+__global__ void __launch_bounds__(kGraphSamples)
+    k_graph_modes(const uint32_t* __restrict__ label, const uint64_t* __restrict__ mbase,
+                  const uint64_t* __restrict__ msize, const uint32_t* __restrict__ mk,
+                  uint32_t* groot) {
+  __shared__ uint32_t a[kGraphSamples];
+  const uint32_t t = threadIdx.x;
+  const uint64_t b = mbase[blockIdx.x], sz = msize[blockIdx.x];
+  const uint64_t seed = hash64(sz + 1);
+  a[t] = label[b + hash64(t + seed) % sz];
+  __syncthreads();
+  for (uint32_t k = 2; k <= (uint32_t)kGraphSamples; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      const uint32_t p = t ^ j;
+      if (p > t) {
+        const uint32_t x = a[t], y = a[p];
+        if ((x > y) == ((t & k) == 0)) {
+          a[t] = y;
+          a[p] = x;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (t == 0) {
+    uint32_t best = a[0], best_cnt = 0;
+    for (uint32_t i = 0; i < (uint32_t)kGraphSamples;) {
+      uint32_t j = 1;
+      while (i + j < (uint32_t)kGraphSamples && a[i + j] == a[i]) j++;
+      if (j > best_cnt) {
+        best_cnt = j;
+        best = a[i];
+      }
+      i += j;
+    }
+    groot[mk[blockIdx.x]] = best;
+  }
+}
+
+// Roots of the given labels after a compressing pass: groot[k] = label[groot[k]].
+__global__ void k_gather_roots(const uint32_t* __restrict__ label, const uint32_t* __restrict__ mk,
+                               uint32_t count, uint32_t* groot) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
+    groot[mk[j]] = label[groot[mk[j]]];
+}
+
 // LDD tree edges (v, parent[v]) for v != parent[v], appended to the forest.
 __global__ void k_ldd_tree_edges(const uint32_t* __restrict__ tree, uint64_t n, uint32_t* forest,
                                  Counters* ctr) {
@@ -555,24 +606,51 @@ __global__ void k_ldd_tree_edges(const uint32_t* __restrict__ tree, uint64_t n, 
   }
 }
 
-// LDD into d_label (centre ids); tree (optional) receives BFS parents.
+// Graphs of a batch with at least one vertex (the whole graph when the
+// handle holds no batch): their vertex bases and sizes.
+static void ldd_members(const psc_graph_s* g, std::vector<uint64_t>& base,
+                        std::vector<uint64_t>& size) {
+  base.clear();
+  size.clear();
+  if (g->num_graphs > 1) {
+    for (uint32_t k = 0; k < g->num_graphs; k++)
+      if (g->vbase[k + 1] > g->vbase[k]) {
+        base.push_back(g->vbase[k]);
+        size.push_back(g->vbase[k + 1] - g->vbase[k]);
+      }
+  } else {
+    base.push_back(0);
+    size.push_back(g->n);
+  }
+}
+
+// LDD into d_label (centre ids); tree (optional) receives BFS parents.  In a
+// batch every graph draws its own candidate centres (hash32(1024 + i) % n_k,
+// as a graph alone would) and all graphs add them on the same schedule, so
+// the centre list is laid out sample-major: entry i * G + k.
 int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
   const uint64_t n = g->n, m = g->m, nwords = (n + 31) / 32;
   const unsigned tb = kCcBlock;
+  std::vector<uint64_t> mb, ms;
+  ldd_members(g, mb, ms);
+  const uint64_t G = mb.size();
+  const uint64_t ncent = (uint64_t)kLddSamples * G;
   uint32_t *qa, *qb, *fa, *fb, *perm, *samp_idx, *samp;
-  PSC_TRY(ensure_t(g, B_QA, n + kLddSamples + 1, &qa));
-  PSC_TRY(ensure_t(g, B_QB, n + kLddSamples + 1, &qb));
+  PSC_TRY(ensure_t(g, B_QA, n + ncent + 1, &qa));
+  PSC_TRY(ensure_t(g, B_QB, n + ncent + 1, &qb));
   PSC_TRY(ensure_t(g, B_FB_A, nwords + 1, &fa));
   PSC_TRY(ensure_t(g, B_FB_B, nwords + 1, &fb));
-  PSC_TRY(ensure_t(g, B_AUX2, kLddSamples + 2 * kMaxLabelSamples, &perm));
-  samp_idx = perm + kLddSamples;
+  PSC_TRY(ensure_t(g, B_AUX2, ncent + 2 * kMaxLabelSamples, &perm));
+  samp_idx = perm + ncent;
   samp = samp_idx + kMaxLabelSamples;
   // centres and label samples, hashed on the host (ldd.hpp:463-466,
   // Connectivity.h:16-20)
-  std::vector<uint32_t> hp(kLddSamples + kMaxLabelSamples);
-  for (int i = 0; i < kLddSamples; i++) hp[i] = (uint32_t)(hash32(kLddSamples + i) % n);
+  std::vector<uint32_t> hp(ncent + kMaxLabelSamples);
+  for (int i = 0; i < kLddSamples; i++)
+    for (uint64_t k = 0; k < G; k++)
+      hp[(uint64_t)i * G + k] = (uint32_t)(mb[k] + hash32(kLddSamples + i) % ms[k]);
   const uint64_t seed = hash64(n + 1);
-  for (int i = 0; i < kMaxLabelSamples; i++) hp[kLddSamples + i] = (uint32_t)(hash64(i + seed) % n);
+  for (int i = 0; i < kMaxLabelSamples; i++) hp[ncent + i] = (uint32_t)(hash64(i + seed) % n);
   PSC_CUDA(cudaMemcpyAsync(perm, hp.data(), hp.size() * 4, cudaMemcpyHostToDevice, g->stream));
   {
     ProfScope ps(g, F_CC);
@@ -593,9 +671,9 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
       PSC_TRY(zero_counters(g));
       k_set_u64<<<1, 1, 0, g->stream>>>(&g->ctr[1].next, pull ? 0ull : (unsigned long long)nf);
       ProfScope ps(g, F_CC);
-      k_ldd_centres<<<grid_for(g, work, 256), 256, 0, g->stream>>>(perm, sampled, work, d_label,
-                                                                   pull ? nullptr : qa,
-                                                                   pull ? fa : nullptr, g->ctr + 1);
+      k_ldd_centres<<<grid_for(g, work * G, 256), 256, 0, g->stream>>>(
+          perm, (uint32_t)(sampled * G), (uint32_t)(work * G), d_label, pull ? nullptr : qa,
+          pull ? fa : nullptr, g->ctr + 1);
       sampled += work;
       PSC_TRY(read_counters(g));
       nf = pull ? nf + g->hctr[1].next : g->hctr[1].next;
@@ -673,24 +751,50 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
   uint32_t* tree = nullptr;
   if (d_forest) PSC_TRY(ensure_t(g, B_TMP32, n + 1, &tree));
   PSC_TRY(ldd_run(g, beta, d_label, tree));
-  uint32_t* samp = (uint32_t*)g->bufs[B_AUX2].p + kLddSamples + kMaxLabelSamples;
-  // most frequent sampled label (Connectivity.h:21-33): ties go to the
-  // smallest label, as the reference's scan of the sorted samples does
-  std::vector<uint32_t> hs(kMaxLabelSamples);
-  PSC_CUDA(cudaMemcpyAsync(hs.data(), samp, kMaxLabelSamples * 4, cudaMemcpyDeviceToHost,
-                           g->stream));
-  PSC_CUDA(cudaStreamSynchronize(g->stream));
-  std::sort(hs.begin(), hs.end());
-  uint32_t max_label = 0, max_cnt = 0;
-  for (size_t i = 0; i < hs.size();) {
-    size_t j = 1;
-    while (i + j < hs.size() && hs[i + j] == hs[i]) j++;
-    if (j > max_cnt) {
-      max_cnt = (uint32_t)j;
-      max_label = hs[i];
+  std::vector<uint64_t> mb, ms;
+  ldd_members(g, mb, ms);
+  const bool batched = g->num_graphs > 1;
+  const uint64_t ncent = (uint64_t)kLddSamples * mb.size();
+  uint32_t* samp = (uint32_t*)g->bufs[B_AUX2].p + ncent + kMaxLabelSamples;
+  uint32_t max_label = 0;
+  uint32_t *groot = nullptr, *mk = nullptr;
+  const uint32_t G = (uint32_t)mb.size();
+  if (batched) {
+    // a batch: each graph's most frequent cluster, sampled on the device
+    uint64_t* mw;
+    PSC_TRY(ensure_t(g, B_GRAPHS, 2 * (size_t)G + (size_t)g->num_graphs + G + 2, &mw));
+    groot = (uint32_t*)(mw + 2 * (size_t)G);
+    mk = groot + g->num_graphs + 1;
+    std::vector<uint64_t> hm(2 * (size_t)G);
+    std::vector<uint32_t> hk;
+    for (uint32_t k = 0; k < g->num_graphs; k++)
+      if (g->vbase[k + 1] > g->vbase[k]) hk.push_back(k);
+    std::copy(mb.begin(), mb.end(), hm.begin());
+    std::copy(ms.begin(), ms.end(), hm.begin() + G);
+    PSC_CUDA(cudaMemcpyAsync(mw, hm.data(), hm.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    PSC_CUDA(cudaMemcpyAsync(mk, hk.data(), hk.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    ProfScope ps(g, F_UF);
+    k_graph_modes<<<G, kGraphSamples, 0, g->stream>>>(d_label, mw, mw + G, mk, groot);
+  } else {
+    // most frequent sampled label (Connectivity.h:21-33): ties go to the
+    // smallest label, as the reference's scan of the sorted samples does
+    std::vector<uint32_t> hs(kMaxLabelSamples);
+    PSC_CUDA(cudaMemcpyAsync(hs.data(), samp, kMaxLabelSamples * 4, cudaMemcpyDeviceToHost,
+                             g->stream));
+    PSC_CUDA(cudaStreamSynchronize(g->stream));
+    std::sort(hs.begin(), hs.end());
+    uint32_t max_cnt = 0;
+    for (size_t i = 0; i < hs.size();) {
+      size_t j = 1;
+      while (i + j < hs.size() && hs[i + j] == hs[i]) j++;
+      if (j > max_cnt) {
+        max_cnt = (uint32_t)j;
+        max_label = hs[i];
+      }
+      i += j;
     }
-    i += j;
   }
+  const uint32_t* gid = batched ? g->d_gid : nullptr;
   // LDD labels are centre ids and every centre labels itself, so the label
   // array is already a depth-1 union-find forest; max_label is its own root.
   PSC_TRY(zero_counters(g));
@@ -714,21 +818,27 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
   {
     ProfScope ps(g, F_UF);
     k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(
-        g->off, g->E, n, d_label, cluster, max_label, 0, kUfSample, forest, g->ctr);
+        g->off, g->E, n, d_label, cluster, max_label, gid, groot, 0, kUfSample, forest, g->ctr);
   }
   {
     ProfScope ps(g, F_UF);
     k_uf_final<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, n);
   }
-  PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux1, d_label + max_label, 4, cudaMemcpyDeviceToHost,
-                           g->stream));
-  PSC_CUDA(cudaStreamSynchronize(g->stream));
   uint32_t max_root = 0;
-  std::memcpy(&max_root, &g->hctr->aux1, 4);
+  if (batched) {
+    ProfScope ps(g, F_UF);
+    k_gather_roots<<<(G + 255) / 256, 256, 0, g->stream>>>(d_label, mk, G, groot);
+  } else {
+    PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux1, d_label + max_label, 4, cudaMemcpyDeviceToHost,
+                             g->stream));
+    PSC_CUDA(cudaStreamSynchronize(g->stream));
+    std::memcpy(&max_root, &g->hctr->aux1, 4);
+  }
   {
     ProfScope ps(g, F_UF);
     k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(
-        g->off, g->E, n, d_label, cluster, max_root, kUfSample, 0xFFFFFFFFu, forest, g->ctr);
+        g->off, g->E, n, d_label, cluster, max_root, gid, groot, kUfSample, 0xFFFFFFFFu, forest,
+        g->ctr);
   }
   {
     ProfScope ps(g, F_UF);

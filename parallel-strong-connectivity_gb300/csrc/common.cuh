@@ -46,6 +46,7 @@ enum Family : int {
   F_TRANSPOSE,
   F_BATCH,
   F_UF,
+  F_LE_SORT,
   F_COUNT
 };
 extern const char* const kFamilyName[F_COUNT];

@@ -13,7 +13,8 @@ namespace psc {
 const char* const kFamilyName[F_COUNT] = {
     "trim",        "reach_push", "reach_pull", "reach_vgc", "heavy",     "label_first",
     "compact",     "ms_seed",    "ms_expand",  "ms_vgc",    "table",     "partition",
-    "finalise",    "cc",         "lelist",     "transpose",  "batch",     "union_find"};
+    "finalise",    "cc",         "lelist",     "transpose",  "batch",     "union_find",
+    "lelist_sort"};
 
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 

@@ -712,14 +712,14 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   PSC_TRY(ensure_t(g, B_P, L + 1, &tgt));
   PSC_CUDA(cudaMemsetAsync(cnt, 0, (n + 1) * 4, g->stream));
   {
-    ProfScope ps(g, F_LE);
+    ProfScope ps(g, F_LE_SORT);
     k_le_count<<<grid_for(g, L, tb), tb, 0, g->stream>>>(Lk, L, cnt);
   }
-  PSC_TRY(scan_emit(g, n, CountValue{cnt}, BucketOffsets{boff, cursor}, nullptr, F_LE));
+  PSC_TRY(scan_emit(g, n, CountValue{cnt}, BucketOffsets{boff, cursor}, nullptr, F_LE_SORT));
   g->hctr[3].aux1 = L;  // boff[n] = L (pinned staging word)
   PSC_CUDA(cudaMemcpyAsync(boff + n, &g->hctr[3].aux1, 8, cudaMemcpyHostToDevice, g->stream));
   {
-    ProfScope ps(g, F_LE);
+    ProfScope ps(g, F_LE_SORT);
     k_le_scatter<<<grid_for(g, L, tb), tb, 0, g->stream>>>(Lk, Ld, L, boff, cursor, Bk);
   }
   PSC_TRY(zero_counters(g));
@@ -736,7 +736,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
     PSC_TRY(ensure_t(g, B_AUX2, slen * sgrid, &scratch));
   }
   {
-    ProfScope ps(g, F_LE);
+    ProfScope ps(g, F_LE_SORT);
     k_seg_sort_u64<<<sgrid, kSegBlock, 0, g->stream>>>(boff, n, Bk, scratch, slen);
     k_le_filter<<<grid_for(g, n, tb), tb, 0, g->stream>>>(boff, n, Bk, keep);
     k_le_target<<<grid_for(g, n, tb), tb, 0, g->stream>>>(boff, n, tgt);
@@ -744,7 +744,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   uint32_t* out;
   PSC_TRY(ensure_t(g, B_AUX0, 3 * L + 3, &out));
   uint64_t kept = 0;
-  PSC_TRY(scan_emit(g, L, KeepValue{keep}, TripleEmit{Bk, tgt, centers, out}, &kept, F_LE));
+  PSC_TRY(scan_emit(g, L, KeepValue{keep}, TripleEmit{Bk, tgt, centers, out}, &kept, F_LE_SORT));
   *len_out = kept;
   return PSC_OK;
 }

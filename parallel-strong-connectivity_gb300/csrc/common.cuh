@@ -145,6 +145,8 @@ enum Buf : int {
   B_FB_B,         // u32[n/32] frontier bitmap B
   B_HEAVY,        // heavy list
   B_SCAN,         // scan scratch
+  B_SCAN2,        // radix offsets of the device transpose
+  B_SCAN3,        // run starts of the device transpose
   B_TMP32,        // u32[n] misc
   B_TF,           // forward label table
   B_TB,           // backward label table

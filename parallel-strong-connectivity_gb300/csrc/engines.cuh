@@ -17,9 +17,8 @@ int batch_attach(psc_graph_s* g, const uint64_t* vbase, uint32_t num_graphs, boo
 int call_begin(psc_graph_s* g);
 int call_end(psc_graph_s* g);
 
-// Builds in_off/in_E from off/E on the device; in-lists sorted by source
-// when `sorted`, else in scatter order (enough for every solver here).
-int build_transpose(psc_graph_s* g, bool sorted = true);
+// Builds in_off/in_E from off/E on the device (in-lists sorted by source).
+int build_transpose(psc_graph_s* g);
 
 // Single-source reachability into the bitmap vis (u32[ceil(n/32)], cleared
 // here).  backward = expand over the transpose.  rounds receives the number

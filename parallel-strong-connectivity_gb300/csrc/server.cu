@@ -54,11 +54,12 @@ struct Request {
   uint32_t batch_size = 0;
 };
 
-// Device bytes a request may need while its batch runs: graph arrays (and the
-// transpose with its build scratch for SCC), labels and the solver's scratch
-// (pivot order, queues, bitmaps, label tables) per vertex.
-uint64_t request_bytes(int kind, uint64_t n, uint64_t m) {
-  if (kind == PSC_REQ_SCC) return 16 * (n + 1) + 12 * m + 160 * n;
+// Device bytes a request may need while its batch runs: graph arrays (and for
+// SCC the transpose, plus its build scratch when it is not sent along),
+// labels and the solver's scratch (pivot order, queues, bitmaps, label
+// tables) per vertex.
+uint64_t request_bytes(int kind, uint64_t n, uint64_t m, bool with_t) {
+  if (kind == PSC_REQ_SCC) return 16 * (n + 1) + (with_t ? 8 : 22) * m + 168 * n;
   return 8 * (n + 1) + 4 * m + 64 * n;
 }
 
@@ -160,8 +161,8 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* lau
     }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(stamp("upload"));
-    // SCC needs the in-edges (not their order) when they did not come along
-    if (kind == PSC_REQ_SCC && !with_t) PSC_TRY(build_transpose(g, false));
+    // SCC needs the in-edges: built on the device when they did not come along
+    if (kind == PSC_REQ_SCC && !with_t) PSC_TRY(build_transpose(g));
     PSC_TRY(batch_attach(g, vbase.data(), R, false));
     PSC_TRY(stamp("transpose"));
     if (kind == PSC_REQ_SCC) {
@@ -309,7 +310,7 @@ extern "C" int psc_server_submit(psc_server_t S, int kind, const uint64_t* off, 
   if (off[0] != 0 || off[n] != m) return PSC_ERR_INVALID;
   if ((in_off && m && !in_E) || (!in_off && in_E)) return PSC_ERR_INVALID;
   if (in_off && (kind != PSC_REQ_SCC || in_off[0] != 0 || in_off[n] != m)) return PSC_ERR_INVALID;
-  const uint64_t bytes = request_bytes(kind, n, m);
+  const uint64_t bytes = request_bytes(kind, n, m, in_off != nullptr);
   auto* r = new Request();
   r->kind = kind;
   r->n = n;

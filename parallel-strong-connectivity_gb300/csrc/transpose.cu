@@ -1,19 +1,11 @@
-// Device transpose (make_directed, src/graph.hpp:222-245): in-degree count,
-// exclusive scan into in_off, then a scatter of every edge u -> v to
-// in_E[in_off[v] + k] through per-target atomic cursors, then a per-list sort
-// so in-lists come out ordered by source as the reference's sort-based
-// transpose leaves them.
+// Device transpose (make_directed, src/graph.hpp:222-245): the in-lists,
+// sorted by source as the reference's sort-based transpose leaves them, from
+// a stable radix sort of the (target, source) pairs by target.
 #include "common.cuh"
 #include "engines.cuh"
 #include "scan.cuh"
 
 namespace psc {
-
-__global__ void k_indeg(const uint32_t* __restrict__ E, uint64_t m, uint32_t* cnt) {
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m;
-       j += (uint64_t)gridDim.x * blockDim.x)
-    atomicAdd(&cnt[E[j]], 1u);
-}
 
 struct CntValue {
   const uint32_t* cnt;
@@ -29,174 +21,261 @@ struct OffEmit {
   }
 };
 
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
-    k_scatter(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E, uint64_t n,
-              const uint64_t* __restrict__ in_off, uint32_t* cursor, uint32_t* in_E) {
-  __shared__ WarpExpandSmem sm[BLOCK / 32];
-  __shared__ uint32_t s_u[BLOCK];
+// ---------------------------------------------------------------------------
+// Radix transpose: the (target, source) pairs of all edges, generated in CSR
+// order (sorted by source), sorted by target with a stable LSD radix sort of
+// kRsBits-bit digits.  Stability keeps every in-list ordered by source, as
+// the reference's sort-based transpose leaves it.  Each pass: a per-tile
+// digit histogram in shared memory, one scan over (digit, tile), and a stable
+// scatter in which every warp ranks its sub-tile with __match_any_sync.  No
+// global atomics, so hub targets cost nothing extra.
+// ---------------------------------------------------------------------------
+constexpr int kRsBits = 8;
+constexpr int kRsBins = 1 << kRsBits;
+constexpr int kRsBlock = 256;
+constexpr int kRsTile = 4096;  // pairs per block and pass (16 per thread)
+
+// src[e] = the vertex whose adjacency holds edge e.  A warp takes 32 * 32
+// consecutive edges; the sources of its first and last edge bound a small
+// vertex range (one vertex for a hub), which every lane's binary search then
+// covers; stores are coalesced.
+constexpr int kSrcRun = 32 * 32;
+
+__device__ __forceinline__ uint64_t edge_owner(const uint64_t* __restrict__ off, uint64_t lo,
+                                               uint64_t hi, uint64_t e) {
+  while (lo < hi) {  // largest u in [lo, hi] with off[u] <= e
+    const uint64_t mid = (lo + hi + 1) >> 1;
+    if (__ldg(&off[mid]) <= e)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_edge_sources(const uint64_t* __restrict__ off, uint64_t n, uint64_t m,
+                               uint32_t* src) {
+  const unsigned lane = lane_id();
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t runs = (m + kSrcRun - 1) / kSrcRun;
+  for (uint64_t r = gw; r < runs; r += nw) {
+    const uint64_t e0 = r * kSrcRun;
+    const uint64_t e1 = e0 + kSrcRun < m ? e0 + kSrcRun : m;
+    uint64_t b = 0;
+    if (lane == 0) b = edge_owner(off, 0, n - 1, e0);
+    if (lane == 1) b = edge_owner(off, 0, n - 1, e1 - 1);
+    const uint64_t lo = __shfl_sync(kFull, b, 0), hi = __shfl_sync(kFull, b, 1);
+    for (uint64_t e = e0 + lane; e < e1; e += 32) src[e] = (uint32_t)edge_owner(off, lo, hi, e);
+  }
+}
+
+// Per-tile digit histograms.  Every thread holds kRsPer keys of its warp's
+// sub-tile in registers (loaded first, so their latencies overlap); equal
+// digits of a warp add to the shared histogram once.
+constexpr int kRsPer = kRsTile / kRsBlock;  // 16 keys per thread
+
+__global__ void __launch_bounds__(kRsBlock)
+    k_rs_hist(const uint32_t* __restrict__ keys, uint64_t m, int shift, uint64_t ntiles,
+              uint32_t* hist) {
+  __shared__ uint32_t cnt[kRsBins];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
-  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
-  for (uint64_t base = gw * 32; base < n; base += nw * 32) {
-    const uint64_t u = base + lane;
-    uint64_t beg = 0;
-    uint64_t deg = 0;
-    if (u < n) {
-      beg = off[u];
-      deg = off[u + 1] - beg;
-    }
-    s_u[wid * 32 + lane] = (uint32_t)u;
-    __syncwarp();
-    // lists in pieces of at most 2^26 edges keep the 32-lane degree sum of
-    // the warp expansion below 2^31
-    while (__any_sync(kFull, deg > 0)) {
-      uint32_t piece = (uint32_t)(deg > (1ull << 26) ? (1ull << 26) : deg);
-      warp_expand(sm[wid], beg, piece, [&](bool act, int s, uint64_t e) {
-        if (act) {
-          const uint32_t v = E[e];
-          const uint32_t k = atomicAdd(&cursor[v], 1u);
-          in_E[in_off[v] + k] = s_u[wid * 32 + s];
-        }
-      });
-      beg += piece;
-      deg -= piece;
-    }
-    __syncwarp();
-  }
-}
-
-// Sorts each in-list.  Lists up to kSmemSort entries: one block, bitonic
-// network in shared memory.  Longer lists: the block runs the same network
-// over global memory.
-constexpr int kSortBlock = 512;
-constexpr int kSmemSort = 4096;
-
-__device__ void bitonic_sort_span(uint32_t* a, uint32_t len, uint32_t pad) {
-  // a has room for `pad` (power of two >= len) entries; the tail is filled
-  // with 0xFFFFFFFF so it sorts last.
-  for (uint32_t i = len + threadIdx.x; i < pad; i += blockDim.x) a[i] = 0xFFFFFFFFu;
-  __syncthreads();
-  for (uint32_t k = 2; k <= pad; k <<= 1) {
-    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-      for (uint32_t i = threadIdx.x; i < pad; i += blockDim.x) {
-        uint32_t p = i ^ j;
-        if (p > i) {
-          uint32_t x = a[i], y = a[p];
-          bool up = (i & k) == 0;
-          if ((x > y) == up) {
-            a[i] = y;
-            a[p] = x;
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kSortBlock)
-    k_sort_lists(const uint64_t* __restrict__ in_off, uint64_t n, uint32_t* in_E, uint32_t* gscratch,
-                 uint64_t scratch_len) {
-  __shared__ uint32_t buf[kSmemSort];
-  for (uint64_t v = blockIdx.x; v < n; v += gridDim.x) {
-    const uint64_t b = in_off[v], e = in_off[v + 1];
-    const uint64_t len = e - b;
-    if (len < 2) continue;
-    if (len <= 32) {
-      // one warp: odd-even transposition sort, one element per lane
-      if (threadIdx.x < 32) {
-        const int t = (int)threadIdx.x;
-        uint32_t x = t < (int)len ? in_E[b + t] : 0xFFFFFFFFu;
-        for (int r = 0; r < 32; r++) {
-          int partner = ((t & 1) == (r & 1)) ? t + 1 : t - 1;
-          uint32_t y = __shfl_sync(kFull, x, partner & 31);
-          if (partner >= 0 && partner < 32) {
-            bool low = t < partner;
-            x = low ? min(x, y) : max(x, y);
-          }
-        }
-        if (t < (int)len) in_E[b + t] = x;
-      }
-      __syncthreads();
-      continue;
-    }
-    uint32_t pad = 64;
-    while (pad < len) pad <<= 1;
-    if (pad <= kSmemSort) {
-      for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) buf[i] = in_E[b + i];
-      bitonic_sort_span(buf, (uint32_t)len, pad);
-      for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) in_E[b + i] = buf[i];
-      __syncthreads();
-    } else if (pad <= scratch_len) {
-      uint32_t* a = gscratch + (uint64_t)blockIdx.x * scratch_len;
-      for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) a[i] = in_E[b + i];
-      __syncthreads();
-      bitonic_sort_span(a, (uint32_t)len, pad);
-      for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) in_E[b + i] = a[i];
-      __syncthreads();
-    }
-  }
-}
-
-__global__ void k_max_len(const uint64_t* __restrict__ in_off, uint64_t n, unsigned long long* out) {
-  unsigned long long mx = 0;
-  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    unsigned long long l = in_off[v + 1] - in_off[v];
-    mx = l > mx ? l : mx;
-  }
+  const unsigned lt = (1u << lane) - 1;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int b = threadIdx.x; b < kRsBins; b += kRsBlock) cnt[b] = 0;
+    __syncthreads();
+    const uint64_t base = tile * kRsTile + (uint64_t)wid * (kRsTile / (kRsBlock / 32));
+    uint32_t d[kRsPer];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long t = __shfl_xor_sync(kFull, mx, o);
-    mx = t > mx ? t : mx;
+    for (int c = 0; c < kRsPer; c++) {
+      const uint64_t i = base + c * 32 + lane;
+      d[c] = i < m ? (__ldg(&keys[i]) >> shift) & (kRsBins - 1) : kRsBins;
+    }
+#pragma unroll
+    for (int c = 0; c < kRsPer; c++) {
+      const unsigned peers = __match_any_sync(kFull, d[c]);
+      if (d[c] < (uint32_t)kRsBins && (peers & lt) == 0) atomicAdd(&cnt[d[c]], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kRsBins; b += kRsBlock) hist[(uint64_t)b * ntiles + tile] = cnt[b];
+    __syncthreads();
   }
-  if ((threadIdx.x & 31) == 0 && mx) atomicMax(out, mx);
 }
 
-int build_transpose(psc_graph_s* g, bool sorted) {
+// Stable scatter of one pass.  Each warp owns kRsTile / 8 consecutive pairs
+// of the tile (chunks of 32 in order, lanes in order), held in registers.
+// The tile is first sorted by digit in shared memory (warp counts, a block
+// scan over digits, ranked placement), then written out so that consecutive
+// threads write consecutive positions of one digit's run: coalesced stores
+// instead of one sector per pair.
+__global__ void __launch_bounds__(kRsBlock)
+    k_rs_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t m,
+                 int shift, uint64_t ntiles, const uint64_t* __restrict__ offs, uint32_t* kout,
+                 uint32_t* vout) {
+  constexpr int NW = kRsBlock / 32;
+  constexpr int PER_WARP = kRsTile / NW;
+  static_assert(kRsBins == kRsBlock, "one digit per thread in the digit scan");
+  __shared__ uint32_t skey[kRsTile];
+  __shared__ uint32_t sval[kRsTile];
+  __shared__ uint32_t wcnt[NW][kRsBins];
+  __shared__ uint32_t lstart[kRsBins];
+  __shared__ uint64_t gbase[kRsBins];
+  __shared__ uint64_t scan_sm[33];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5, tid = threadIdx.x;
+  const unsigned lt = (1u << lane) - 1;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint64_t tbase = tile * kRsTile;
+    const uint64_t base = tbase + (uint64_t)wid * PER_WARP;
+    const uint32_t tcount = (uint32_t)(m - tbase < (uint64_t)kRsTile ? m - tbase : kRsTile);
+    uint32_t key[kRsPer], val[kRsPer], d[kRsPer];
+#pragma unroll
+    for (int c = 0; c < kRsPer; c++) {
+      const uint64_t i = base + c * 32 + lane;
+      key[c] = 0;
+      val[c] = 0;
+      d[c] = kRsBins;
+      if (i < m) {
+        key[c] = __ldg(&kin[i]);
+        val[c] = __ldg(&vin[i]);
+        d[c] = (key[c] >> shift) & (kRsBins - 1);
+      }
+    }
+    for (int b = lane; b < kRsBins; b += 32) wcnt[wid][b] = 0;
+    __syncwarp();
+    unsigned peers[kRsPer];
+#pragma unroll
+    for (int c = 0; c < kRsPer; c++) {
+      peers[c] = __match_any_sync(kFull, d[c]);
+      if (d[c] < (uint32_t)kRsBins && (peers[c] & lt) == 0) wcnt[wid][d[c]] += __popc(peers[c]);
+      __syncwarp();
+    }
+    __syncthreads();
+    // digit tid: its start in the sorted tile, each warp's base inside it, and
+    // the global start of its run for this tile
+    {
+      uint32_t total = 0;
+#pragma unroll
+      for (int w = 0; w < NW; w++) total += wcnt[w][tid];
+      uint64_t all = 0;
+      const uint32_t start = (uint32_t)block_excl_scan<kRsBlock>(total, scan_sm, &all);
+      lstart[tid] = start;
+      gbase[tid] = offs[(uint64_t)tid * ntiles + tile];
+      uint32_t run = start;
+#pragma unroll
+      for (int w = 0; w < NW; w++) {
+        const uint32_t c = wcnt[w][tid];
+        wcnt[w][tid] = run;
+        run += c;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kRsPer; c++) {
+      uint32_t lp = 0;
+      if (d[c] < (uint32_t)kRsBins) lp = wcnt[wid][d[c]] + __popc(peers[c] & lt);
+      __syncwarp();
+      if (d[c] < (uint32_t)kRsBins) {
+        skey[lp] = key[c];
+        sval[lp] = val[c];
+        if ((peers[c] & lt) == 0) wcnt[wid][d[c]] += __popc(peers[c]);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < tcount; j += kRsBlock) {
+      const uint32_t k = skey[j];
+      const uint32_t dj = (k >> shift) & (kRsBins - 1);
+      const uint64_t pos = gbase[dj] + (j - lstart[dj]);
+      kout[pos] = k;
+      vout[pos] = sval[j];
+    }
+    __syncthreads();
+  }
+}
+
+struct HistValue {
+  const uint32_t* hist;
+  __device__ uint32_t operator()(uint64_t i) const { return hist[i]; }
+};
+
+struct HistEmit {
+  uint64_t* offs;
+  __device__ void operator()(uint64_t i, uint64_t excl, uint32_t) const { offs[i] = excl; }
+};
+
+// In-degrees from the sorted targets: run starts record their position,
+// run ends turn it into the run length.
+__global__ void k_run_starts(const uint32_t* __restrict__ t, uint64_t m, uint64_t* rs) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    if (i == 0 || t[i - 1] != t[i]) rs[t[i]] = i;
+}
+
+__global__ void k_run_lengths(const uint32_t* __restrict__ t, uint64_t m,
+                              const uint64_t* __restrict__ rs, uint32_t* cnt) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    if (i == m - 1 || t[i + 1] != t[i]) cnt[t[i]] = (uint32_t)(i + 1 - rs[t[i]]);
+}
+
+int build_transpose(psc_graph_s* g) {
   const uint64_t n = g->n, m = g->m;
   uint32_t* cnt;
   PSC_TRY(ensure_t(g, B_TMP32, n + 1, &cnt));
   PSC_CUDA(cudaMemsetAsync(cnt, 0, (n + 1) * 4, g->stream));
-  {
-    ProfScope ps(g, F_TRANSPOSE);
-    ps.bytes = 8.0 * m;
-    k_indeg<<<grid_for(g, m, 256), 256, 0, g->stream>>>(g->E, m, cnt);
+  if (m > 0) {
+    int bits = 1;
+    while (bits < 32 && ((uint64_t)1 << bits) < n) bits++;
+    const int passes = (bits + kRsBits - 1) / kRsBits;
+    const uint64_t ntiles = (m + kRsTile - 1) / kRsTile;
+    uint32_t *x, *ka, *kb, *hist;
+    uint64_t* offs;
+    PSC_TRY(ensure_t(g, B_AUX0, m, &x));
+    PSC_TRY(ensure_t(g, B_AUX1, m, &ka));
+    PSC_TRY(ensure_t(g, B_AUX2, m, &kb));
+    PSC_TRY(ensure_t(g, B_AUX3, (uint64_t)kRsBins * ntiles, &hist));
+    PSC_TRY(ensure_t(g, B_SCAN2, (uint64_t)kRsBins * ntiles + 1, &offs));
+    // value buffers alternate so that the last pass writes in_E
+    uint32_t* vb[2] = {passes % 2 ? x : g->in_E, passes % 2 ? g->in_E : x};
+    uint32_t* kbuf[2] = {ka, kb};
+    {
+      ProfScope ps(g, F_TRANSPOSE);
+      ps.bytes = 16.0 * n + 4.0 * m;
+      k_edge_sources<<<grid_for(g, (m + kSrcRun - 1) / kSrcRun * 32, 256), 256, 0, g->stream>>>(
+          g->off, n, m, vb[0]);
+    }
+    const uint32_t* kin = g->E;
+    const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)g->num_sms * 8);
+    for (int p = 0; p < passes; p++) {
+      const int shift = p * kRsBits;
+      {
+        ProfScope ps(g, F_TRANSPOSE);
+        ps.bytes = 4.0 * m;
+        k_rs_hist<<<grid, kRsBlock, 0, g->stream>>>(kin, m, shift, ntiles, hist);
+      }
+      PSC_TRY(scan_emit(g, (uint64_t)kRsBins * ntiles, HistValue{hist}, HistEmit{offs}, nullptr,
+                        F_TRANSPOSE));
+      {
+        ProfScope ps(g, F_TRANSPOSE);
+        ps.bytes = 16.0 * m;
+        k_rs_scatter<<<grid, kRsBlock, 0, g->stream>>>(kin, vb[p & 1], m, shift, ntiles, offs,
+                                                       kbuf[p & 1], vb[(p + 1) & 1]);
+      }
+      kin = kbuf[p & 1];
+    }
+    uint64_t* rs;
+    PSC_TRY(ensure_t(g, B_SCAN3, n + 1, &rs));
+    {
+      ProfScope ps(g, F_TRANSPOSE);
+      ps.bytes = 8.0 * m;
+      k_run_starts<<<grid_for(g, m, 256), 256, 0, g->stream>>>(kin, m, rs);
+      k_run_lengths<<<grid_for(g, m, 256), 256, 0, g->stream>>>(kin, m, rs, cnt);
+    }
   }
-  // in_off[i] = prefix of counts; the count array doubles as the cursor
-  // (reset to zero by the emit step after it is read).
   uint64_t total = 0;
   PSC_TRY(scan_emit(g, n, CntValue{cnt}, OffEmit{g->in_off, cnt}, &total, F_TRANSPOSE));
   PSC_CUDA(cudaMemcpyAsync(g->in_off + n, &g->m, 8, cudaMemcpyHostToDevice, g->stream));
-  {
-    ProfScope ps(g, F_TRANSPOSE);
-    ps.bytes = 16.0 * n + 16.0 * m;
-    k_scatter<256><<<grid_for(g, n, 256), 256, 0, g->stream>>>(g->off, g->E, n, g->in_off, cnt,
-                                                               g->in_E);
-  }
-  if (!sorted) return PSC_OK;
-  // longest in-list decides the global scratch of the sort
-  PSC_TRY(zero_counters(g));
-  k_max_len<<<grid_for(g, n, 256), 256, 0, g->stream>>>(g->in_off, n, &g->ctr->aux0);
-  PSC_TRY(read_counters(g));
-  const uint64_t maxlen = g->hctr->aux0;
-  uint64_t pad = 64;
-  while (pad < maxlen) pad <<= 1;
-  const unsigned sort_grid = (unsigned)std::min<uint64_t>(n, (uint64_t)g->num_sms * 4);
-  uint32_t* scratch = nullptr;
-  uint64_t scratch_len = 0;
-  if (pad > (uint64_t)kSmemSort) {
-    scratch_len = pad;
-    PSC_TRY(ensure_t(g, B_AUX3, scratch_len * sort_grid, &scratch));
-  }
-  {
-    ProfScope ps(g, F_TRANSPOSE);
-    ps.bytes = 8.0 * m;
-    k_sort_lists<<<sort_grid, kSortBlock, 0, g->stream>>>(g->in_off, n, g->in_E, scratch, scratch_len);
-  }
   PSC_CUDA(cudaGetLastError());
-  (void)total;
   return PSC_OK;
 }
 

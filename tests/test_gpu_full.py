@@ -30,6 +30,13 @@ def test_scc_knn_full(knn):
     assert np.array_equal(O.canon(lab), O.canon(tar))
 
 
+def test_device_transpose_knn_full(knn):
+    """Three radix passes (ids of 24 bits) over 5 * 10^7 edges."""
+    with psc.DeviceGraph.directed(knn.off, knn.E) as dg:
+        in_off, in_E = dg.transpose()
+    assert np.array_equal(in_off, knn.in_off) and np.array_equal(in_E, knn.in_E)
+
+
 def test_scc_grid_full():
     g = psc.HostGraph.grid(4096, 4096, 0.3, seed=2)
     with psc.DeviceGraph(g) as dg:

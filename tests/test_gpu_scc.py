@@ -130,6 +130,20 @@ def test_device_transpose_heavy_lists():
     assert np.array_equal(in_off, g.in_off) and np.array_equal(in_E, g.in_E)
 
 
+@pytest.mark.parametrize("n,m,seed", [(1, 0, 1), (7, 0, 2), (100, 900, 3), (300, 50, 4),
+                                      ((1 << 17) + 3, 600000, 5), (1 << 20, 40000, 6)])
+def test_device_transpose_sizes(n, m, seed):
+    """Radix passes 1 to 3 (target ids up to 8, 9, 18, 20 bits), edgeless
+    graphs and long runs of vertices without in-edges."""
+    rng = np.random.default_rng(seed)
+    src = rng.integers(0, n, m).astype(np.uint32)
+    dst = (rng.integers(0, max(1, n // 7), m) * 7 % n).astype(np.uint32)  # sparse targets
+    g = psc.HostGraph.from_edges(n, src, dst)
+    with psc.DeviceGraph.directed(g.off, g.E) as dg:
+        in_off, in_E = dg.transpose()
+    assert np.array_equal(in_off, g.in_off) and np.array_equal(in_E, g.in_E)
+
+
 def test_invalid_source_rejected():
     g = generated("rmat", 10, 1)
     with psc.DeviceGraph(g) as dg:

@@ -82,7 +82,7 @@ def test_server_matches_plain_calls():
 def test_server_budget_admission():
     reqs = stream(24, seed0=9, lo=9, hi=11)
     # room for about two requests at a time
-    big = max(16 * (g.n + 1) + 12 * g.m + 160 * g.n for g, _, _ in reqs)
+    big = max(16 * (g.n + 1) + 22 * g.m + 168 * g.n for g, _, _ in reqs)
     budget = 2 * big + 1
     with psc.Server(workers=4, max_batch=64, hbm_budget=budget) as srv:
         ids = [srv.submit(g, kind, seed) for g, kind, seed in reqs]

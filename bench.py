@@ -51,6 +51,9 @@ WORKLOADS = {
                    make=lambda psc: psc.HostGraph.rmat(16, 1 << 20, seed=1)),
     "rmat26": dict(desc="directed R-MAT n=2^26, 2^30 draws (0.57,0.19,0.19,0.05), seed 3, dedup",
                    make=lambda psc: psc.HostGraph.rmat(26, 1 << 30, seed=3)),
+    "rmat22": dict(desc="directed R-MAT n=2^22, 2^26 draws (0.57,0.19,0.19,0.05), seed 3, dedup "
+                        "(a profiling size of the 2^26 configuration)",
+                   make=lambda psc: psc.HostGraph.rmat(22, 1 << 26, seed=3)),
 }
 
 
@@ -300,13 +303,27 @@ def run_ncu_step(args) -> None:
         return
     wl = WORKLOADS[args.workload]
     g = wl["make"](psc)
-    with psc.DeviceGraph(g) as dg:
-        params = psc.default_params(seed=1)
+    if args.ncu_op == "scc":
+        with psc.DeviceGraph(g) as dg:
+            params = psc.default_params(seed=1)
+            for _ in range(2):
+                dg.scc(params)
+            st = dg.stats()
+    elif args.ncu_op == "transpose":
         for _ in range(2):
-            dg.scc(params)
-        st = dg.stats()
-        log(f"ncu step: {args.workload} n={g.n} m={g.m} {st.total_ms:.2f} ms, "
-            f"{st.kernel_launches} launches")
+            with psc.DeviceGraph.directed(g.off, g.E) as dg:
+                st = dg.stats()
+    else:
+        s = g.symmetrize()
+        with psc.DeviceGraph(s) as dg:
+            for _ in range(2):
+                if args.ncu_op == "cc":
+                    dg.cc()
+                else:
+                    dg.lelist(psc.random_permutation(s.n, 4))
+            st = dg.stats()
+    log(f"ncu step: {args.ncu_op} on {args.workload} n={g.n} m={g.m} {st.total_ms:.2f} ms, "
+        f"{st.kernel_launches} launches")
 
 
 BATCH = dict(seed0=1000, log2_min=8.0, log2_max=18.0)
@@ -900,6 +917,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-step", action="store_true",
                     help="profiling target: one warm-up solve and one solve only")
+    ap.add_argument("--ncu-op", choices=["scc", "cc", "lelist", "transpose"], default="scc",
+                    help="operation of --ncu-step (cc and lelist on the symmetrised graph)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "psc":
         log("note: fewer than 3 warm-up steps")

@@ -19,6 +19,7 @@
 // The result is the reference's list, and seq_le_list's (LeList.hpp:76-115).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 
 #include "common.cuh"
@@ -286,14 +287,69 @@ __global__ void k_le_seed(const uint32_t* __restrict__ centers, uint64_t start, 
   }
 }
 
+// Pairs whose vertex has more than `hthr` edges are expanded by k_le_heavy,
+// balanced over the whole grid, instead of by one warp.  They are listed with
+// one 64-bit atomic on ctr->heavy = count << kLeHeavyShift | edge offset, so
+// list order and edge offsets agree: Hs is increasing and entry h owns the
+// virtual edges [Hs[h], Hs[h + 1]).
+constexpr uint64_t kLeHeavy = 256;
+constexpr int kLeHeavyShift = 40;
+constexpr uint64_t kLeHeavyMask = (1ull << kLeHeavyShift) - 1;
+
+// Offers the warp's K candidate pairs key[k] = (p, w[k]) (kEmpty: none):
+// new pairs go to the next frontier and become list entries (w, p, level),
+// and lower next_dist[w].  Called by all 32 lanes.
+template <int K>
+__device__ __forceinline__ void le_offer(const uint64_t* __restrict__ off, const uint32_t (&w)[K],
+                                         const uint64_t (&key)[K], uint32_t level,
+                                         unsigned long long* T, uint64_t mask, uint64_t* Fout,
+                                         uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld,
+                                         Counters* ctr, uint32_t& probes,
+                                         unsigned long long& next_edges) {
+  const unsigned lane = lane_id();
+  uint32_t tm = 0;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (key[k] != kEmpty && table_insert(T, mask, key[k], 0xFFFFFFFFu, &probes) == 1) {
+      tm |= 1u << k;
+      atomicMin(&next_dist[w[k]], level);
+    }
+  const uint32_t cnt = __popc(tm);
+  uint32_t pinc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, pinc, o);
+    if ((int)lane >= o) pinc += t;
+  }
+  const uint32_t tot = __shfl_sync(kFull, pinc, 31);
+  if (!tot) return;
+  unsigned long long fb = 0, lb = 0;
+  if (lane == 31) {
+    fb = atomicAdd(&ctr->next, (unsigned long long)tot);
+    lb = atomicAdd(&ctr->aux1, (unsigned long long)tot);
+  }
+  fb = __shfl_sync(kFull, fb, 31) + (pinc - cnt);
+  lb = __shfl_sync(kFull, lb, 31) + (pinc - cnt);
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (tm & (1u << k)) {
+      Fout[fb++] = key[k];
+      Lk[lb] = ((uint64_t)w[k] << 32) | (key[k] >> 32);
+      Ld[lb++] = level;
+      next_edges += off[w[k] + 1] - off[w[k]];
+    }
+}
+
 // One level of a batch: frontier pairs (p, u); every edge (u, w) with
-// level < dist[w] offers (p, w).
+// level < dist[w] offers (p, w).  A warp expands 32 pairs together; pairs
+// with more than hthr edges are listed for k_le_heavy.
 template <int BLOCK, int K>
 __global__ void __launch_bounds__(BLOCK)
     k_le_expand(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
                 const uint32_t* __restrict__ dist, const uint64_t* __restrict__ Fin, uint64_t nf,
                 uint32_t level, unsigned long long* T, uint64_t mask, uint64_t* Fout,
-                uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld, Counters* ctr) {
+                uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld, uint64_t hthr, uint64_t* Hk,
+                uint64_t* Hs, Counters* ctr) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ uint32_t s_p[BLOCK];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -311,6 +367,14 @@ __global__ void __launch_bounds__(BLOCK)
       p = (uint32_t)(key >> 32);
       beg = off[u];
       rem = off[u + 1] - beg;
+      if (rem > hthr) {
+        const unsigned long long old =
+            atomicAdd(&ctr->heavy, (1ull << kLeHeavyShift) + (unsigned long long)rem);
+        const uint64_t h = old >> kLeHeavyShift;
+        Hk[h] = key;
+        Hs[h] = old & kLeHeavyMask;
+        rem = 0;
+      }
     }
     scanned += rem;
     s_p[wid * 32 + lane] = p;
@@ -327,7 +391,7 @@ __global__ void __launch_bounds__(BLOCK)
       sm[wid].beg[lane] = beg;
       __syncwarp();
       for (uint32_t b = 0; b < total; b += 32 * K) {
-        uint32_t w[K], src[K], tm = 0;
+        uint32_t w[K], src[K];
         uint64_t key[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
@@ -353,43 +417,72 @@ __global__ void __launch_bounds__(BLOCK)
           if (w[k] != kNone && level < __ldg(&dist[w[k]]))
             key[k] = ((uint64_t)s_p[wid * 32 + src[k]] << 32) | w[k];
         }
-#pragma unroll
-        for (int k = 0; k < K; k++)
-          if (key[k] != kEmpty && table_insert(T, mask, key[k], 0xFFFFFFFFu, &probes) == 1) {
-            tm |= 1u << k;
-            atomicMin(&next_dist[w[k]], level);
-          }
-        // new pairs: next frontier and list entries (w, p, level)
-        const uint32_t cnt = __popc(tm);
-        uint32_t pinc = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t t = __shfl_up_sync(kFull, pinc, o);
-          if ((int)lane >= o) pinc += t;
-        }
-        const uint32_t tot = __shfl_sync(kFull, pinc, 31);
-        if (tot) {
-          unsigned long long fb = 0, lb = 0;
-          if (lane == 31) {
-            fb = atomicAdd(&ctr->next, (unsigned long long)tot);
-            lb = atomicAdd(&ctr->aux1, (unsigned long long)tot);
-          }
-          fb = __shfl_sync(kFull, fb, 31) + (pinc - cnt);
-          lb = __shfl_sync(kFull, lb, 31) + (pinc - cnt);
-#pragma unroll
-          for (int k = 0; k < K; k++)
-            if (tm & (1u << k)) {
-              Fout[fb++] = key[k];
-              Lk[lb] = ((uint64_t)w[k] << 32) | (key[k] >> 32);
-              Ld[lb++] = level;
-              next_edges += off[w[k] + 1] - off[w[k]];
-            }
-        }
+        le_offer<K>(off, w, key, level, T, mask, Fout, next_dist, Lk, Ld, ctr, probes,
+                    next_edges);
       }
       __syncwarp();
       beg += deg;
       rem -= deg;
     }
+  }
+  scanned = warp_sum(scanned);
+  next_edges = warp_sum(next_edges);
+  unsigned long long pr = warp_sum((unsigned long long)probes);
+  if (lane == 0) {
+    if (scanned) atomicAdd(&ctr->edges, scanned);
+    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
+    if (pr) atomicAdd(&ctr->probes, pr);
+  }
+}
+
+// The heavy pairs of a level: the grid walks their concatenated edge lists,
+// 32 * K consecutive edges per warp step (an entry has more than 32 * K edges,
+// so a step spans at most two entries).
+template <int BLOCK, int K>
+__global__ void __launch_bounds__(BLOCK)
+    k_le_heavy(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
+               const uint32_t* __restrict__ dist, const uint64_t* __restrict__ Hk,
+               const uint64_t* __restrict__ Hs, uint32_t level, unsigned long long* T,
+               uint64_t mask, uint64_t* Fout, uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld,
+               Counters* ctr) {
+  const unsigned long long packed = ctr->heavy;
+  const uint64_t nh = packed >> kLeHeavyShift, total = packed & kLeHeavyMask;
+  if (nh == 0) return;
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  unsigned long long scanned = 0, next_edges = 0;
+  uint32_t probes = 0;
+  for (uint64_t x0 = gw * 32 * K; x0 < total; x0 += nw * 32 * K) {
+    uint64_t lo = 0, hi = nh - 1;  // last entry with Hs <= x0
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi + 1) >> 1;
+      if (__ldg(&Hs[mid]) <= x0)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    uint32_t w[K];
+    uint64_t key[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint64_t x = x0 + k * 32 + lane;
+      w[k] = kNone;
+      key[k] = kEmpty;
+      if (x < total) {
+        uint64_t h = lo;
+        while (h + 1 < nh && __ldg(&Hs[h + 1]) <= x) h++;
+        const uint64_t pk = __ldg(&Hk[h]);
+        const uint32_t u = (uint32_t)pk;
+        const uint32_t v = __ldg(&E[off[u] + (x - __ldg(&Hs[h]))]);
+        scanned++;
+        if (level < __ldg(&dist[v])) {
+          w[k] = v;
+          key[k] = (pk & 0xFFFFFFFF00000000ull) | v;
+        }
+      }
+    }
+    le_offer<K>(off, w, key, level, T, mask, Fout, next_dist, Lk, Ld, ctr, probes, next_edges);
   }
   scanned = warp_sum(scanned);
   next_edges = warp_sum(next_edges);
@@ -445,12 +538,59 @@ __global__ void k_le_scatter(const uint64_t* __restrict__ Lk, const uint32_t* __
   }
 }
 
-// Sorts every bucket [boff[v], boff[v+1]) of u64 values ascending: one warp
-// per bucket up to 32 entries (odd-even transposition in registers), a block
+// Sorts every bucket [boff[v], boff[v+1]) of u64 values ascending.  Buckets
+// of at most kSegThread entries (nearly all of them: a vertex's list candidates
+// number a few) are sorted by one thread each with a compare-exchange network
+// in registers, and the longer ones are listed; a block then sorts each listed
+// bucket: one warp up to 32 entries (odd-even transposition in registers), a
 // bitonic network in shared memory up to kSegSmem entries, and the same
 // network over a global scratch row beyond that.
 constexpr int kSegBlock = 256;
 constexpr int kSegSmem = 2048;
+constexpr int kSegThread = 16;
+
+template <int S>
+__device__ __forceinline__ void sort_net_u64(uint64_t* B, uint64_t b, uint32_t len) {
+  uint64_t a[S];
+#pragma unroll
+  for (int i = 0; i < S; i++) a[i] = i < (int)len ? B[b + i] : ~0ull;
+#pragma unroll
+  for (int i = 1; i < S; i++)
+#pragma unroll
+    for (int j = i; j > 0; j--) {
+      const uint64_t x = a[j - 1], y = a[j];
+      a[j - 1] = x < y ? x : y;
+      a[j] = x < y ? y : x;
+    }
+#pragma unroll
+  for (int i = 0; i < S; i++)
+    if (i < (int)len) B[b + i] = a[i];
+}
+
+// Small buckets sorted in place; longer ones appended to big[] (count in
+// ctr->heavy); the longest length goes to ctr->aux0.
+__global__ void k_seg_sort_small(const uint64_t* __restrict__ boff, uint64_t nseg, uint64_t* B,
+                                 uint32_t* big, Counters* ctr) {
+  unsigned long long mx = 0;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nseg;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = boff[v], len = boff[v + 1] - b;
+    mx = len > mx ? len : mx;
+    if (len < 2) continue;
+    if (len <= 4)
+      sort_net_u64<4>(B, b, (uint32_t)len);
+    else if (len <= kSegThread)
+      sort_net_u64<kSegThread>(B, b, (uint32_t)len);
+    else
+      big[atomicAdd(&ctr->heavy, 1ull)] = (uint32_t)v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(kFull, mx, o);
+    mx = t > mx ? t : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(&ctr->aux0, mx);
+}
 
 __device__ void bitonic_u64(uint64_t* a, uint32_t len, uint32_t pad) {
   for (uint32_t i = len + threadIdx.x; i < pad; i += blockDim.x) a[i] = ~0ull;
@@ -474,12 +614,13 @@ __device__ void bitonic_u64(uint64_t* a, uint32_t len, uint32_t pad) {
 }
 
 __global__ void __launch_bounds__(kSegBlock)
-    k_seg_sort_u64(const uint64_t* __restrict__ boff, uint64_t nseg, uint64_t* B, uint64_t* scratch,
+    k_seg_sort_u64(const uint32_t* __restrict__ big, uint64_t nbig,
+                   const uint64_t* __restrict__ boff, uint64_t* B, uint64_t* scratch,
                    uint64_t scratch_len) {
   __shared__ uint64_t buf[kSegSmem];
-  for (uint64_t v = blockIdx.x; v < nseg; v += gridDim.x) {
+  for (uint64_t k = blockIdx.x; k < nbig; k += gridDim.x) {
+    const uint32_t v = big[k];
     const uint64_t b = boff[v], len = boff[v + 1] - b;
-    if (len < 2) continue;
     if (len <= 32) {
       if (threadIdx.x < 32) {
         const int t = (int)threadIdx.x;
@@ -510,22 +651,6 @@ __global__ void __launch_bounds__(kSegBlock)
       __syncthreads();
     }
   }
-}
-
-__global__ void k_seg_maxlen(const uint64_t* __restrict__ boff, uint64_t nseg,
-                             unsigned long long* out) {
-  unsigned long long mx = 0;
-  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nseg;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    const unsigned long long l = boff[v + 1] - boff[v];
-    mx = l > mx ? l : mx;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_xor_sync(kFull, mx, o);
-    mx = t > mx ? t : mx;
-  }
-  if ((threadIdx.x & 31) == 0 && mx) atomicMax(out, mx);
 }
 
 // Keep an entry if its distance is below every earlier priority's in its
@@ -677,15 +802,52 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
         FB = (uint64_t*)g->bufs[B_PB].p;
       }
       PSC_TRY(le_list_reserve(g, L + bound, L, &lcap));
+      // heavy list: at most bound / (hthr + 1) <= 2^23 entries (count field)
+      // over at most bound < 2^40 edges (offset field)
+      if (bound >> kLeHeavyShift) return PSC_ERR_CAPACITY;
+      const uint64_t hthr = std::max<uint64_t>(kLeHeavy, bound >> 23);
+      const bool any_heavy = bound > hthr;
+      uint64_t *Hk = nullptr, *Hs = nullptr;
+      if (any_heavy) {
+        const uint64_t hcap = std::min<uint64_t>(nf, bound / (hthr + 1)) + 1;
+        PSC_TRY(ensure_t(g, B_PA2, hcap, &Hk));
+        PSC_TRY(ensure_t(g, B_PB2, hcap, &Hs));
+      }
       PSC_TRY(zero_counters(g));
       {
         ProfScope ps(g, F_LE);
+        uint64_t* Lk = (uint64_t*)g->bufs[B_PH].p + L;
+        uint32_t* Ld = (uint32_t*)g->bufs[B_AUX3].p + L;
         k_le_expand<kLeBlock, kLeK><<<grid_for(g, nf, kLeBlock), kLeBlock, 0, g->stream>>>(
-            g->off, g->E, dist, FA, nf, level, T, cap - 1, FB, next_dist,
-            (uint64_t*)g->bufs[B_PH].p + L, (uint32_t*)g->bufs[B_AUX3].p + L, g->ctr);
+            g->off, g->E, dist, FA, nf, level, T, cap - 1, FB, next_dist, Lk, Ld,
+            any_heavy ? hthr : ~0ull, Hk, Hs, g->ctr);
+        if (any_heavy) {
+          const uint64_t hblocks = (bound + kLeBlock * kLeK - 1) / (kLeBlock * kLeK);
+          const unsigned hgrid =
+              (unsigned)std::min<uint64_t>(hblocks, (uint64_t)g->num_sms * 2048 / kLeBlock);
+          k_le_heavy<kLeBlock, kLeK><<<hgrid, kLeBlock, 0, g->stream>>>(
+              g->off, g->E, dist, Hk, Hs, level, T, cap - 1, FB, next_dist, Lk, Ld, g->ctr);
+        }
       }
       PSC_CUDA(cudaGetLastError());
+      cudaEvent_t tr_b = nullptr;
+      const bool tr = trace_on();
+      if (tr) {
+        tr_b = take_event(g);
+        PSC_CUDA(cudaEventRecord(tr_b, g->stream));
+      }
       PSC_TRY(read_counters(g));
+      if (tr) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, g->t0, tr_b);
+        give_event(g, tr_b);
+        std::fprintf(stderr, "le batch %llu [%llu,%llu) level %u nf %llu edges %llu new %llu "
+                     "probes %llu cap %llu t %.3f ms\n",
+                     (unsigned long long)g->stats.batches, (unsigned long long)start,
+                     (unsigned long long)end, level, (unsigned long long)nf,
+                     g->hctr[0].edges, g->hctr[0].next, g->hctr[0].probes,
+                     (unsigned long long)cap, ms);
+      }
       const uint64_t added = g->hctr[0].next;
       ne += added;
       L += added;
@@ -722,13 +884,18 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
     ProfScope ps(g, F_LE_SORT);
     k_le_scatter<<<grid_for(g, L, tb), tb, 0, g->stream>>>(Lk, Ld, L, boff, cursor, Bk);
   }
+  uint32_t* big;
+  PSC_TRY(ensure_t(g, B_QA, n + 1, &big));
   PSC_TRY(zero_counters(g));
-  k_seg_maxlen<<<grid_for(g, n, 256), 256, 0, g->stream>>>(boff, n, &g->ctr->aux0);
+  {
+    ProfScope ps(g, F_LE_SORT);
+    k_seg_sort_small<<<grid_for(g, n, tb), tb, 0, g->stream>>>(boff, n, Bk, big, g->ctr);
+  }
   PSC_TRY(read_counters(g));
-  const uint64_t maxlen = g->hctr[0].aux0;
+  const uint64_t maxlen = g->hctr[0].aux0, nbig = g->hctr[0].heavy;
   uint64_t pad = 64;
   while (pad < maxlen) pad <<= 1;
-  const unsigned sgrid = (unsigned)std::min<uint64_t>(n, (uint64_t)g->num_sms * 8);
+  const unsigned sgrid = (unsigned)std::min<uint64_t>(nbig, (uint64_t)g->num_sms * 8);
   uint64_t* scratch = nullptr;
   uint64_t slen = 0;
   if (pad > (uint64_t)kSegSmem) {
@@ -737,7 +904,8 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   }
   {
     ProfScope ps(g, F_LE_SORT);
-    k_seg_sort_u64<<<sgrid, kSegBlock, 0, g->stream>>>(boff, n, Bk, scratch, slen);
+    if (nbig)
+      k_seg_sort_u64<<<sgrid, kSegBlock, 0, g->stream>>>(big, nbig, boff, Bk, scratch, slen);
     k_le_filter<<<grid_for(g, n, tb), tb, 0, g->stream>>>(boff, n, Bk, keep);
     k_le_target<<<grid_for(g, n, tb), tb, 0, g->stream>>>(boff, n, tgt);
   }

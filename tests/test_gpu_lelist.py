@@ -51,6 +51,33 @@ def test_lelist_generated(kind, size, seed):
             assert np.array_equal(dg.lelist(perm, beta), ref)
 
 
+def hub_graph(n, sizes, seed):
+    """Symmetric graph: hubs 0..len(sizes) with the given numbers of random
+    neighbours over a sparse random backbone."""
+    rng = np.random.default_rng(seed)
+    src, dst = [], []
+    for h, size in enumerate(sizes):
+        src.append(np.full(size, h))
+        dst.append(rng.choice(np.arange(len(sizes), n), size, replace=False))
+    src.append(rng.integers(0, n, 2 * n))
+    dst.append(rng.integers(0, n, 2 * n))
+    return psc.HostGraph.from_edges(n, np.concatenate(src), np.concatenate(dst)).symmetrize()
+
+
+@pytest.mark.parametrize("sizes,seed", [((6000, 3000, 1000, 300, 257), 17),
+                                        ((40000,), 3), (tuple([400] * 64), 8)])
+def test_lelist_heavy_pairs(sizes, seed):
+    """Vertices with hundreds to tens of thousands of edges (expanded by the
+    balanced heavy-pair kernel) reached by many priorities at several levels;
+    one frontier may hold many heavy pairs of the same hub."""
+    s = hub_graph(50_000, sizes, seed)
+    perm = psc.random_permutation(s.n, seed)
+    ref = O.lelist_seq(s.n, s.off, s.E, perm)
+    with psc.DeviceGraph(s) as dg:
+        for beta in (1.5, 4.0):
+            assert np.array_equal(dg.lelist(perm, beta), ref)
+
+
 def test_lelist_directed_matches_definition():
     """Distances follow out-edges: the device result equals seq_le_list's
     definition on a directed graph too."""

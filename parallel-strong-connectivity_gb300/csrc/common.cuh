@@ -107,6 +107,7 @@ struct psc_graph_s {
   int vgc_blocks = 0;     // resident blocks per SM of the reach VGC kernel
   int ms_vgc_blocks = 0;  // same for the multi-search VGC kernel
   int ldd_vgc_blocks = 0; // same for the LDD VGC kernel
+  int le_heavy_blocks = 0; // same for the LE-list heavy-pair kernel
   uint32_t block = 0;     // threads per block of the expansion kernels (0: 256)
   // named scratch buffers, grown on demand (stream-ordered allocator)
   std::vector<psc::DevBuf> bufs;

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "common.cuh"
 #include "engines.cuh"
@@ -294,25 +295,33 @@ __global__ void k_le_seed(const uint32_t* __restrict__ centers, uint64_t start, 
 // virtual edges [Hs[h], Hs[h + 1]).
 constexpr uint64_t kLeHeavy = 256;
 constexpr int kLeHeavyShift = 40;
+constexpr uint32_t kLeProbes = 256;  // probe limit of a sized-by-estimate level
 constexpr uint64_t kLeHeavyMask = (1ull << kLeHeavyShift) - 1;
 
 // Offers the warp's K candidate pairs key[k] = (p, w[k]) (kEmpty: none):
 // new pairs go to the next frontier and become list entries (w, p, level),
-// and lower next_dist[w].  Called by all 32 lanes.
+// and lower next_dist[w]; an insert that gives up after `limit` probes is
+// counted in `fails` (the level is then run again on a larger table).  Called
+// by all 32 lanes.
 template <int K>
 __device__ __forceinline__ void le_offer(const uint64_t* __restrict__ off, const uint32_t (&w)[K],
                                          const uint64_t (&key)[K], uint32_t level,
-                                         unsigned long long* T, uint64_t mask, uint64_t* Fout,
-                                         uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld,
-                                         Counters* ctr, uint32_t& probes,
-                                         unsigned long long& next_edges) {
+                                         unsigned long long* T, uint64_t mask, uint32_t limit,
+                                         uint64_t* Fout, uint32_t* next_dist, uint64_t* Lk,
+                                         uint32_t* Ld, Counters* ctr, uint32_t& probes,
+                                         uint32_t& fails, unsigned long long& next_edges) {
   const unsigned lane = lane_id();
   uint32_t tm = 0;
 #pragma unroll
   for (int k = 0; k < K; k++)
-    if (key[k] != kEmpty && table_insert(T, mask, key[k], 0xFFFFFFFFu, &probes) == 1) {
-      tm |= 1u << k;
-      atomicMin(&next_dist[w[k]], level);
+    if (key[k] != kEmpty) {
+      const int r = table_insert(T, mask, key[k], limit, &probes);
+      if (r == 1) {
+        tm |= 1u << k;
+        atomicMin(&next_dist[w[k]], level);
+      } else if (r < 0) {
+        fails++;
+      }
     }
   const uint32_t cnt = __popc(tm);
   uint32_t pinc = cnt;
@@ -347,16 +356,16 @@ template <int BLOCK, int K>
 __global__ void __launch_bounds__(BLOCK)
     k_le_expand(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
                 const uint32_t* __restrict__ dist, const uint64_t* __restrict__ Fin, uint64_t nf,
-                uint32_t level, unsigned long long* T, uint64_t mask, uint64_t* Fout,
-                uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld, uint64_t hthr, uint64_t* Hk,
-                uint64_t* Hs, Counters* ctr) {
+                uint32_t level, unsigned long long* T, uint64_t mask, uint32_t limit,
+                uint64_t* Fout, uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld, uint64_t hthr,
+                uint64_t* Hk, uint64_t* Hs, Counters* ctr) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ uint32_t s_p[BLOCK];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   unsigned long long scanned = 0, next_edges = 0;
-  uint32_t probes = 0;
+  uint32_t probes = 0, fails = 0;
   for (uint64_t base = gw * 32; base < nf; base += nw * 32) {
     const uint64_t i = base + lane;
     uint64_t beg = 0, rem = 0;
@@ -417,8 +426,8 @@ __global__ void __launch_bounds__(BLOCK)
           if (w[k] != kNone && level < __ldg(&dist[w[k]]))
             key[k] = ((uint64_t)s_p[wid * 32 + src[k]] << 32) | w[k];
         }
-        le_offer<K>(off, w, key, level, T, mask, Fout, next_dist, Lk, Ld, ctr, probes,
-                    next_edges);
+        le_offer<K>(off, w, key, level, T, mask, limit, Fout, next_dist, Lk, Ld, ctr, probes,
+                    fails, next_edges);
       }
       __syncwarp();
       beg += deg;
@@ -427,40 +436,59 @@ __global__ void __launch_bounds__(BLOCK)
   }
   scanned = warp_sum(scanned);
   next_edges = warp_sum(next_edges);
-  unsigned long long pr = warp_sum((unsigned long long)probes);
+  const unsigned long long pr = warp_sum((unsigned long long)probes);
+  const unsigned long long nfail = warp_sum((unsigned long long)fails);
   if (lane == 0) {
     if (scanned) atomicAdd(&ctr->edges, scanned);
     if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
     if (pr) atomicAdd(&ctr->probes, pr);
+    if (nfail) atomicAdd(&ctr->fail, nfail);
   }
 }
 
-// The heavy pairs of a level: the grid walks their concatenated edge lists,
-// 32 * K consecutive edges per warp step (an entry has more than 32 * K edges,
-// so a step spans at most two entries).
+// The heavy pairs of a level: their edge lists, concatenated, are cut into
+// one contiguous slice per warp of a resident grid.  A warp finds the entry at
+// the start of its slice once, then walks 32 * K edges per step with the
+// entry's data held warp-uniform; an entry has more than 32 * K edges, so a
+// step spans at most two entries.
 template <int BLOCK, int K>
 __global__ void __launch_bounds__(BLOCK)
     k_le_heavy(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
                const uint32_t* __restrict__ dist, const uint64_t* __restrict__ Hk,
                const uint64_t* __restrict__ Hs, uint32_t level, unsigned long long* T,
-               uint64_t mask, uint64_t* Fout, uint32_t* next_dist, uint64_t* Lk, uint32_t* Ld,
-               Counters* ctr) {
+               uint64_t mask, uint32_t limit, uint64_t* Fout, uint32_t* next_dist, uint64_t* Lk,
+               uint32_t* Ld, Counters* ctr) {
+  constexpr uint64_t kStep = 32 * K;
   const unsigned long long packed = ctr->heavy;
   const uint64_t nh = packed >> kLeHeavyShift, total = packed & kLeHeavyMask;
   if (nh == 0) return;
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  const uint64_t slice = ((total + nw - 1) / nw + kStep - 1) / kStep * kStep;
+  const uint64_t x_beg = gw * slice;
+  if (x_beg >= total) return;
+  const uint64_t x_end = x_beg + slice < total ? x_beg + slice : total;
+  uint64_t h = 0, hi = nh - 1;  // last entry with Hs <= x_beg
+  while (h < hi) {
+    const uint64_t mid = (h + hi + 1) >> 1;
+    if (__ldg(&Hs[mid]) <= x_beg)
+      h = mid;
+    else
+      hi = mid - 1;
+  }
+  // entry h: virtual edges [hs, hn), pair key pk, edge list from eb
+  uint64_t hs = __ldg(&Hs[h]), hn = h + 1 < nh ? __ldg(&Hs[h + 1]) : total;
+  uint64_t pk = __ldg(&Hk[h]), eb = off[(uint32_t)pk];
   unsigned long long scanned = 0, next_edges = 0;
-  uint32_t probes = 0;
-  for (uint64_t x0 = gw * 32 * K; x0 < total; x0 += nw * 32 * K) {
-    uint64_t lo = 0, hi = nh - 1;  // last entry with Hs <= x0
-    while (lo < hi) {
-      const uint64_t mid = (lo + hi + 1) >> 1;
-      if (__ldg(&Hs[mid]) <= x0)
-        lo = mid;
-      else
-        hi = mid - 1;
+  uint32_t probes = 0, fails = 0;
+  for (uint64_t x0 = x_beg; x0 < x_end; x0 += kStep) {
+    const bool nxt = x0 + kStep >= hn && h + 1 < nh;
+    uint64_t pk2 = 0, eb2 = 0, hn2 = 0;
+    if (nxt) {
+      pk2 = __ldg(&Hk[h + 1]);
+      eb2 = off[(uint32_t)pk2];
+      hn2 = h + 2 < nh ? __ldg(&Hs[h + 2]) : total;
     }
     uint32_t w[K];
     uint64_t key[K];
@@ -469,28 +497,35 @@ __global__ void __launch_bounds__(BLOCK)
       const uint64_t x = x0 + k * 32 + lane;
       w[k] = kNone;
       key[k] = kEmpty;
-      if (x < total) {
-        uint64_t h = lo;
-        while (h + 1 < nh && __ldg(&Hs[h + 1]) <= x) h++;
-        const uint64_t pk = __ldg(&Hk[h]);
-        const uint32_t u = (uint32_t)pk;
-        const uint32_t v = __ldg(&E[off[u] + (x - __ldg(&Hs[h]))]);
+      if (x < x_end) {
+        const bool second = x >= hn;
+        const uint32_t v = __ldg(&E[second ? eb2 + (x - hn) : eb + (x - hs)]);
         scanned++;
         if (level < __ldg(&dist[v])) {
           w[k] = v;
-          key[k] = (pk & 0xFFFFFFFF00000000ull) | v;
+          key[k] = ((second ? pk2 : pk) & 0xFFFFFFFF00000000ull) | v;
         }
       }
     }
-    le_offer<K>(off, w, key, level, T, mask, Fout, next_dist, Lk, Ld, ctr, probes, next_edges);
+    le_offer<K>(off, w, key, level, T, mask, limit, Fout, next_dist, Lk, Ld, ctr, probes, fails,
+                next_edges);
+    if (nxt) {
+      h++;
+      hs = hn;
+      hn = hn2;
+      pk = pk2;
+      eb = eb2;
+    }
   }
   scanned = warp_sum(scanned);
   next_edges = warp_sum(next_edges);
-  unsigned long long pr = warp_sum((unsigned long long)probes);
+  const unsigned long long pr = warp_sum((unsigned long long)probes);
+  const unsigned long long nfail = warp_sum((unsigned long long)fails);
   if (lane == 0) {
     if (scanned) atomicAdd(&ctr->edges, scanned);
     if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
     if (pr) atomicAdd(&ctr->probes, pr);
+    if (nfail) atomicAdd(&ctr->fail, nfail);
   }
 }
 
@@ -755,6 +790,8 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   // prefix-doubling batches (LeList.hpp:255-276)
   uint64_t step = 1, finished = 1;
   uint64_t prev_ne = n >> 1;
+  // inserts per scanned edge at each level of the previous batch
+  std::vector<double> ratio, ratio_next;
   while (finished < n) {
     step = (uint64_t)std::ceil((double)step * beta);
     if (step < 1) step = 1;
@@ -780,27 +817,40 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
     // out-edges of the seeds bound the first level's inserts
     uint64_t bound = 0;
     PSC_TRY(scan_emit(g, nf0, SeedDeg{g->off, centers, start}, NoEmit{}, &bound, F_LE));
+    // Rehashes the pair set into a table of cap2 slots; the frontiers keep
+    // their first keep_a (current) and keep_b (next) pairs.
+    auto grow = [&](uint64_t cap2, uint64_t keep_a, uint64_t keep_b) -> int {
+      unsigned long long* T2;
+      PSC_TRY(ensure_t(g, B_TS, cap2, &T2));
+      PSC_CUDA(cudaMemsetAsync(T2, 0xFF, cap2 * 8, g->stream));
+      k_le_rehash<<<grid_for(g, cap, 256), 256, 0, g->stream>>>(T, cap, T2, cap2 - 1);
+      swap_bufs(g, B_TF, B_TS);
+      cap = cap2;
+      T = T2;
+      g->stats.table_grows++;
+      void* q;
+      PSC_TRY(ensure_keep(g, B_PA, cap * 8 + 16, keep_a * 8, &q));
+      PSC_TRY(ensure_keep(g, B_PB, cap * 8 + 16, keep_b * 8, &q));
+      FA = (uint64_t*)g->bufs[B_PA].p;
+      FB = (uint64_t*)g->bufs[B_PB].p;
+      return PSC_OK;
+    };
+    ratio_next.clear();
     uint32_t level = 0;
     while (nf > 0) {
       level++;
       g->stats.subrounds++;
-      // every possible insert of this level fits at load <= 1/2
-      if (2 * (ne + bound) > cap) {
-        const uint64_t cap2 = p2(2 * (ne + bound) + 1024);
-        unsigned long long* T2;
-        PSC_TRY(ensure_t(g, B_TS, cap2, &T2));
-        PSC_CUDA(cudaMemsetAsync(T2, 0xFF, cap2 * 8, g->stream));
-        k_le_rehash<<<grid_for(g, cap, 256), 256, 0, g->stream>>>(T, cap, T2, cap2 - 1);
-        swap_bufs(g, B_TF, B_TS);
-        cap = cap2;
-        T = T2;
-        g->stats.table_grows++;
-        void* q;
-        PSC_TRY(ensure_keep(g, B_PA, cap * 8 + 16, nf * 8, &q));
-        PSC_TRY(ensure(g, B_PB, cap * 8 + 16, &q));
-        FA = (uint64_t*)g->bufs[B_PA].p;
-        FB = (uint64_t*)g->bufs[B_PB].p;
-      }
+      // A level inserts at most `bound` pairs (one per scanned edge), far
+      // fewer in practice.  The table is sized for twice the previous batch's
+      // inserts per edge at this level, at load <= 1/2; inserts give up after
+      // kLeProbes probes, and a level that had failures runs again on a table
+      // sized for `bound` (offers are idempotent: pairs already inserted are
+      // not emitted twice), without a probe limit.
+      uint64_t est = bound;
+      if (level <= ratio.size())
+        est = std::min<uint64_t>(bound, (uint64_t)std::ceil(2.0 * ratio[level - 1] * bound) + 4096);
+      bool exact = est == bound;
+      if (2 * (ne + est) > cap) PSC_TRY(grow(p2(2 * (ne + est) + 1024), nf, 0));
       PSC_TRY(le_list_reserve(g, L + bound, L, &lcap));
       // heavy list: at most bound / (hthr + 1) <= 2^23 entries (count field)
       // over at most bound < 2^40 edges (offset field)
@@ -813,42 +863,58 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
         PSC_TRY(ensure_t(g, B_PA2, hcap, &Hk));
         PSC_TRY(ensure_t(g, B_PB2, hcap, &Hs));
       }
+      if (any_heavy && !g->le_heavy_blocks) {
+        PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &g->le_heavy_blocks, k_le_heavy<kLeBlock, kLeK>, kLeBlock, 0));
+        if (g->le_heavy_blocks < 1) g->le_heavy_blocks = 1;
+      }
       PSC_TRY(zero_counters(g));
-      {
-        ProfScope ps(g, F_LE);
-        uint64_t* Lk = (uint64_t*)g->bufs[B_PH].p + L;
-        uint32_t* Ld = (uint32_t*)g->bufs[B_AUX3].p + L;
-        k_le_expand<kLeBlock, kLeK><<<grid_for(g, nf, kLeBlock), kLeBlock, 0, g->stream>>>(
-            g->off, g->E, dist, FA, nf, level, T, cap - 1, FB, next_dist, Lk, Ld,
-            any_heavy ? hthr : ~0ull, Hk, Hs, g->ctr);
-        if (any_heavy) {
-          const uint64_t hblocks = (bound + kLeBlock * kLeK - 1) / (kLeBlock * kLeK);
-          const unsigned hgrid =
-              (unsigned)std::min<uint64_t>(hblocks, (uint64_t)g->num_sms * 2048 / kLeBlock);
-          k_le_heavy<kLeBlock, kLeK><<<hgrid, kLeBlock, 0, g->stream>>>(
-              g->off, g->E, dist, Hk, Hs, level, T, cap - 1, FB, next_dist, Lk, Ld, g->ctr);
+      uint32_t attempts = 0;
+      for (;;) {
+        attempts++;
+        {
+          ProfScope ps(g, F_LE);
+          uint64_t* Lk = (uint64_t*)g->bufs[B_PH].p + L;
+          uint32_t* Ld = (uint32_t*)g->bufs[B_AUX3].p + L;
+          const uint32_t limit = exact ? 0xFFFFFFFFu : kLeProbes;
+          k_le_expand<kLeBlock, kLeK><<<grid_for(g, nf, kLeBlock), kLeBlock, 0, g->stream>>>(
+              g->off, g->E, dist, FA, nf, level, T, cap - 1, limit, FB, next_dist, Lk, Ld,
+              any_heavy ? hthr : ~0ull, Hk, Hs, g->ctr);
+          if (any_heavy) {
+            const uint64_t hblocks = (bound + kLeBlock * kLeK - 1) / (kLeBlock * kLeK);
+            const unsigned hgrid = (unsigned)std::min<uint64_t>(
+                hblocks, (uint64_t)g->num_sms * g->le_heavy_blocks);
+            k_le_heavy<kLeBlock, kLeK><<<hgrid, kLeBlock, 0, g->stream>>>(
+                g->off, g->E, dist, Hk, Hs, level, T, cap - 1, limit, FB, next_dist, Lk, Ld,
+                g->ctr);
+          }
         }
+        PSC_CUDA(cudaGetLastError());
+        PSC_TRY(read_counters(g));
+        if (g->hctr[0].fail == 0) break;
+        if (exact) return PSC_ERR_TABLE_FULL;  // load <= 1/2 without a probe limit: unreachable
+        // the next frontier and the list keep this attempt's new pairs; the
+        // heavy list is rebuilt
+        PSC_TRY(grow(p2(2 * (ne + bound) + 1024), nf, g->hctr[0].next));
+        PSC_CUDA(cudaMemsetAsync(&g->ctr->heavy, 0, 2 * sizeof(unsigned long long), g->stream));
+        exact = true;
       }
-      PSC_CUDA(cudaGetLastError());
-      cudaEvent_t tr_b = nullptr;
-      const bool tr = trace_on();
-      if (tr) {
-        tr_b = take_event(g);
-        PSC_CUDA(cudaEventRecord(tr_b, g->stream));
-      }
-      PSC_TRY(read_counters(g));
-      if (tr) {
+      if (trace_on()) {  // ms since the start of the call (the stream is idle here)
         float ms = 0;
-        cudaEventElapsedTime(&ms, g->t0, tr_b);
-        give_event(g, tr_b);
+        cudaEvent_t ev = take_event(g);
+        PSC_CUDA(cudaEventRecord(ev, g->stream));
+        PSC_CUDA(cudaEventSynchronize(ev));
+        cudaEventElapsedTime(&ms, g->t0, ev);
+        give_event(g, ev);
         std::fprintf(stderr, "le batch %llu [%llu,%llu) level %u nf %llu edges %llu new %llu "
-                     "probes %llu cap %llu t %.3f ms\n",
+                     "probes %llu cap %llu attempts %u t %.3f ms\n",
                      (unsigned long long)g->stats.batches, (unsigned long long)start,
                      (unsigned long long)end, level, (unsigned long long)nf,
                      g->hctr[0].edges, g->hctr[0].next, g->hctr[0].probes,
-                     (unsigned long long)cap, ms);
+                     (unsigned long long)cap, attempts, ms);
       }
       const uint64_t added = g->hctr[0].next;
+      ratio_next.push_back((double)added / (double)std::max<uint64_t>(bound, 1));
       ne += added;
       L += added;
       bound = g->hctr[0].next_edges;
@@ -856,6 +922,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
       swap_bufs(g, B_PA, B_PB);
       nf = added;
     }
+    ratio.swap(ratio_next);
     PSC_CUDA(cudaMemcpyAsync(dist, next_dist, n * 4, cudaMemcpyDeviceToDevice, g->stream));
     prev_ne = (uint64_t)std::ceil((double)ne * beta);
     finished = end;

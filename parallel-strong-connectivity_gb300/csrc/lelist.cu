@@ -30,7 +30,8 @@
 namespace psc {
 
 constexpr int kLeBlock = 256;
-constexpr int kLeK = 4;
+constexpr int kLeK = 4;       // edges in flight per lane: BFS push, heavy pairs
+constexpr int kLeKLight = 8;  // the same for the warp expansion of light pairs
 
 // ---------------------------------------------------------------------------
 // BFS
@@ -877,7 +878,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
           uint64_t* Lk = (uint64_t*)g->bufs[B_PH].p + L;
           uint32_t* Ld = (uint32_t*)g->bufs[B_AUX3].p + L;
           const uint32_t limit = exact ? 0xFFFFFFFFu : kLeProbes;
-          k_le_expand<kLeBlock, kLeK><<<grid_for(g, nf, kLeBlock), kLeBlock, 0, g->stream>>>(
+          k_le_expand<kLeBlock, kLeKLight><<<grid_for(g, nf, kLeBlock), kLeBlock, 0, g->stream>>>(
               g->off, g->E, dist, FA, nf, level, T, cap - 1, limit, FB, next_dist, Lk, Ld,
               any_heavy ? hthr : ~0ull, Hk, Hs, g->ctr);
           if (any_heavy) {

@@ -8,7 +8,8 @@ int ensure_keep(psc_graph_s* g, int b, size_t bytes, size_t keep, void** out);
 // A handle with its stream, counters and events for a graph of n vertices
 // and m edges, and its graph arrays from the stream-ordered pool
 // (in_off/in_E alias off/E when symmetric).
-int make_handle(uint64_t n, uint64_t m, psc_graph_s** out);
+// priority: of the handle's stream (0 = default; lower numbers run first)
+int make_handle(uint64_t n, uint64_t m, psc_graph_s** out, int priority = 0);
 int alloc_graph_arrays(psc_graph_s* g, bool symmetric);
 // Attaches a graph-offset table (vertex bases, host u64[G+1]) to g: the
 // per-vertex graph ids and, when check is set, the test that no edge crosses

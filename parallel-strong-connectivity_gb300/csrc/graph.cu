@@ -162,7 +162,7 @@ int call_end(psc_graph_s* g) {
   return PSC_OK;
 }
 
-int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
+int make_handle(uint64_t n, uint64_t m, psc_graph_s** out, int priority) {
   int dev = 0;
   PSC_CUDA(cudaGetDevice(&dev));
   auto* g = new psc_graph_s();
@@ -172,7 +172,7 @@ int make_handle(uint64_t n, uint64_t m, psc_graph_s** out) {
   g->bufs.resize(B_COUNT);
   cudaError_t e;
   if ((e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithPriority(&g->stream, cudaStreamNonBlocking, priority)) != cudaSuccess ||
       (e = cudaMalloc(&g->ctr, kCounterSets * sizeof(Counters))) != cudaSuccess ||
       (e = cudaMallocHost(&g->hctr, kCounterSets * sizeof(Counters))) != cudaSuccess ||
       (e = cudaEventCreate(&g->t0)) != cudaSuccess || (e = cudaEventCreate(&g->t1)) != cudaSuccess ||

@@ -15,6 +15,10 @@
 // admitted as soon as a worker and enough budget are free, so their work
 // overlaps the running batches on the device.
 //
+// A batch of few edges (up to kUrgentEdges) runs on a high-priority stream: its
+// solve is a chain of small, latency-bound rounds that would otherwise wait
+// behind the wide kernels of the large batches running beside it.
+//
 // A request's result does not depend on the batch it lands in: SCC labels
 // equal psc_scc on the graph alone with the request's seed, connectivity
 // labels give the same partition as psc_cc on the graph alone.
@@ -97,12 +101,15 @@ struct psc_server_s {
   uint64_t next_id = 1;
   uint64_t used = 0;      // bytes admitted by running batches
   uint32_t running = 0;   // batches on the device
+  int urgent_priority = 0;  // stream priority of small batches
   bool stop = false;
   psc_server_stats_t stats{};
 };
 
 namespace psc {
 namespace {
+
+constexpr uint64_t kUrgentEdges = 1ull << 26;
 
 // Solves one batch of requests of the same kind on a fresh handle.
 int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* launches) {
@@ -118,7 +125,7 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* lau
   std::vector<std::pair<const char*, double>> marks;
   const auto t_begin = Clock::now();
   psc_graph_s* g = nullptr;
-  PSC_TRY(make_handle(n, m, &g));
+  PSC_TRY(make_handle(n, m, &g, m <= kUrgentEdges ? S->urgent_priority : 0));
   auto stamp = [&](const char* what) -> int {
     if (!tr) return PSC_OK;
     PSC_CUDA(cudaStreamSynchronize(g->stream));
@@ -293,9 +300,12 @@ extern "C" int psc_server_create(const psc_server_config_t* cfg, psc_server_t* o
     return PSC_ERR_INVALID;
   int dev = 0;
   PSC_CUDA(cudaGetDevice(&dev));
+  int least = 0, greatest = 0;
+  PSC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
   auto* S = new psc_server_s();
   S->cfg = c;
   S->device = dev;
+  S->urgent_priority = greatest;
   for (uint32_t w = 0; w < c.workers; w++) S->workers.emplace_back(worker_loop, S);
   *out = S;
   return PSC_OK;

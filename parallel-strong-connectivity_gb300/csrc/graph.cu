@@ -3,6 +3,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "engines.cuh"
@@ -19,6 +21,47 @@ const char* const kFamilyName[F_COUNT] = {
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+
+// Counter blocks (device + pinned host) are recycled across handles instead
+// of freed: cudaFree and cudaFreeHost synchronize the whole device, which
+// would stall every other stream (the request server's other workers) each
+// time a handle goes away.
+namespace {
+struct CtrBlock {
+  int device;
+  Counters* d;
+  Counters* h;
+};
+std::mutex g_ctr_mu;
+std::vector<CtrBlock> g_ctr_pool;
+
+cudaError_t ctr_take(int dev, Counters** d, Counters** h) {
+  {
+    std::lock_guard<std::mutex> lk(g_ctr_mu);
+    for (size_t i = 0; i < g_ctr_pool.size(); i++)
+      if (g_ctr_pool[i].device == dev) {
+        *d = g_ctr_pool[i].d;
+        *h = g_ctr_pool[i].h;
+        g_ctr_pool[i] = g_ctr_pool.back();
+        g_ctr_pool.pop_back();
+        return cudaSuccess;
+      }
+  }
+  cudaError_t e = cudaMalloc(d, kCounterSets * sizeof(Counters));
+  if (e != cudaSuccess) return e;
+  e = cudaMallocHost(h, kCounterSets * sizeof(Counters));
+  if (e != cudaSuccess) {
+    cudaFree(*d);
+    *d = nullptr;
+  }
+  return e;
+}
+
+void ctr_give(int dev, Counters* d, Counters* h) {
+  std::lock_guard<std::mutex> lk(g_ctr_mu);
+  g_ctr_pool.push_back(CtrBlock{dev, d, h});
+}
+}  // namespace
 
 bool trace_on() {
   static const bool on = [] {
@@ -173,8 +216,7 @@ int make_handle(uint64_t n, uint64_t m, psc_graph_s** out, int priority) {
   cudaError_t e;
   if ((e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
       (e = cudaStreamCreateWithPriority(&g->stream, cudaStreamNonBlocking, priority)) != cudaSuccess ||
-      (e = cudaMalloc(&g->ctr, kCounterSets * sizeof(Counters))) != cudaSuccess ||
-      (e = cudaMallocHost(&g->hctr, kCounterSets * sizeof(Counters))) != cudaSuccess ||
+      (e = ctr_take(dev, &g->ctr, &g->hctr)) != cudaSuccess ||
       (e = cudaEventCreate(&g->t0)) != cudaSuccess || (e = cudaEventCreate(&g->t1)) != cudaSuccess ||
       (e = cudaEventCreate(&g->u0)) != cudaSuccess || (e = cudaEventCreate(&g->u1)) != cudaSuccess ||
       (e = cudaEventCreate(&g->ph[0])) != cudaSuccess || (e = cudaEventCreate(&g->ph[1])) != cudaSuccess ||
@@ -320,8 +362,7 @@ int psc_graph_free(psc_graph_t g) {
   if (g->d_vbase) cudaFreeAsync(g->d_vbase, g->stream);
   if (g->d_gid) cudaFreeAsync(g->d_gid, g->stream);
   if (g->stream) cudaStreamSynchronize(g->stream);
-  if (g->ctr) cudaFree(g->ctr);
-  if (g->hctr) cudaFreeHost(g->hctr);
+  if (g->ctr) ctr_give(g->device, g->ctr, g->hctr);
   for (auto& p : g->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);

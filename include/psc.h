@@ -230,7 +230,7 @@ int psc_server_destroy(psc_server_t s);
  * and no allocating library routine.  Its scratch (visited and frontier
  * bitmaps, two frontier queues, the heavy list and the round counters) is one
  * file-scope __device__ array sized for PSC_NOALLOC_MAX_VERTICES vertices,
- * about 26 MB, which every GPU that loads the library holds until the
+ * about 34 MB, which every GPU that loads the library holds until the
  * process exits.  Larger graphs are rejected with PSC_ERR_TOO_LARGE before
  * any device work.
  *

@@ -23,6 +23,10 @@ constexpr int kWarp = 32;
 // Frontier vertices with more out-edges than this are expanded by the whole
 // grid instead of by one warp.
 constexpr uint32_t kHeavyDeg = 8192;
+// Heavy-list counters: count << kPackShift | work units (edges or chunks),
+// updated with one 64-bit atomic per listed item.
+constexpr int kPackShift = 40;
+constexpr uint64_t kPackMask = (1ull << kPackShift) - 1;
 
 // ---------------------------------------------------------------------------
 // Kernel families for profiling (launch counts, event time, algorithmic bytes)

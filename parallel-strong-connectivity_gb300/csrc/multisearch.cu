@@ -56,6 +56,22 @@ struct MsSide {
   uint32_t vgc_budget;  // new pairs one VGC local search may insert
 };
 
+constexpr int kMsHeavyK = 4;  // heavy pairs: edges in flight per lane
+constexpr uint64_t kMsHeavyChunk = 32 * kMsHeavyK;
+constexpr uint32_t kRequeued = 0x80000000u;  // hflag bit: the pair was re-queued
+
+// Lists a pair whose vertex has more than kHeavyDeg out-edges for k_ms_heavy.
+// Its edges are cut into chunks of kMsHeavyChunk; one 64-bit atomic on
+// ctr->heavy = count << kPackShift | chunks gives the pair its slot and its
+// first chunk (hflag, below the kRequeued bit), increasing with the slot.
+__device__ __forceinline__ void ms_heavy_push(const MsSide& S, uint64_t key, uint64_t deg) {
+  const unsigned long long old = atomicAdd(
+      &S.ctr->heavy, (1ull << kPackShift) + (deg + kMsHeavyChunk - 1) / kMsHeavyChunk);
+  const uint64_t hh = old >> kPackShift;
+  S.Fheavy[hh] = key;
+  S.hflag[hh] = (uint32_t)(old & kPackMask);
+}
+
 // Per-warp source data of one expansion step.
 struct MsSrc {
   uint64_t sub[32];
@@ -281,9 +297,7 @@ __global__ void __launch_bounds__(BLOCK, (768 / BLOCK) > 0 ? (768 / BLOCK) : 1)
       sub = labels[u];
       (sd ? ex1 : ex0)++;
       if (d > kHeavyDeg) {
-        const unsigned long long hh = atomicAdd(&S.ctr->heavy, 1ull);
-        S.Fheavy[hh] = key;
-        S.hflag[hh] = 0;
+        ms_heavy_push(S, key, d);
         d = 0;
       }
       deg = (uint32_t)d;
@@ -444,11 +458,7 @@ __global__ void __launch_bounds__(BLOCK)
     uint32_t probes = 0;
     if (!(du > 0 && du < tq)) {
       if (du > kHeavyDeg) {
-        if (lane == 0) {
-          const unsigned long long hh = atomicAdd(&S.ctr->heavy, 1ull);
-          S.Fheavy[hh] = key;
-          S.hflag[hh] = 0;
-        }
+        if (lane == 0) ms_heavy_push(S, key, du);
         continue;
       }
       // a vertex with tau..kHeavyDeg out-edges: the warp walks them with
@@ -576,48 +586,83 @@ __global__ void __launch_bounds__(BLOCK)
   flush_ms_counters(s0.ctr, s1.ctr, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1, in0, in1);
 }
 
-// Heavy pairs of both sides: the whole grid walks each one's edges.
+// Heavy pairs of both sides: the chunks of a side's heavy list are cut into
+// one contiguous range per warp; a warp finds the pair of its first chunk
+// once, then offers kMsHeavyChunk edges per step (a heavy pair has more than
+// 64 chunks, so the next pair is at most one step away).  A step with a
+// failed insert re-queues its pair once (kRequeued), whichever warp failed
+// first.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_ms_heavy(MsSide s0, MsSide s1, const uint64_t* __restrict__ labels) {
+  constexpr int K = kMsHeavyK;
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const uint64_t stride = (uint64_t)gridDim.x * BLOCK;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
 #pragma unroll 1
   for (int sd = 0; sd < 2; sd++) {
     const MsSide S = sd ? s1 : s0;
     if (!S.ctr) continue;
-    const uint64_t nh = *(volatile unsigned long long*)&S.ctr->heavy;
+    const unsigned long long packed = S.ctr->heavy;
+    const uint64_t nh = packed >> kPackShift, total = packed & kPackMask;
+    const uint64_t per = (total + nw - 1) / nw;
+    const uint64_t c_beg = gw * per, c_end = c_beg + per < total ? c_beg + per : total;
+    if (nh == 0 || c_beg >= c_end) continue;
+    // first chunks: hflag below the kRequeued bit (fixed while other warps set that bit)
+    auto first_chunk = [&](uint64_t i) -> uint64_t { return S.hflag[i] & ~kRequeued; };
+    uint64_t h = 0, hi = nh - 1;  // last pair whose first chunk is <= c_beg
+    while (h < hi) {
+      const uint64_t mid = (h + hi + 1) >> 1;
+      if (first_chunk(mid) <= c_beg)
+        h = mid;
+      else
+        hi = mid - 1;
+    }
+    uint64_t key = S.Fheavy[h], cs = first_chunk(h), cn = h + 1 < nh ? first_chunk(h + 1) : total;
+    uint64_t sub = labels[key >> 32], beg = S.off[key >> 32], end = S.off[(key >> 32) + 1];
     unsigned long long scanned = 0, requeued = 0, ins = 0;
     uint32_t probes = 0;
-    for (uint64_t hh = 0; hh < nh; hh++) {
-      const uint64_t key = S.Fheavy[hh];
-      const uint32_t u = (uint32_t)(key >> 32);
+    for (uint64_t c = c_beg; c < c_end; c++) {
+      if (c >= cn) {
+        h++;
+        key = S.Fheavy[h];
+        cs = cn;
+        cn = h + 1 < nh ? first_chunk(h + 1) : total;
+        sub = labels[key >> 32];
+        beg = S.off[key >> 32];
+        end = S.off[(key >> 32) + 1];
+      }
+      const uint64_t e0 = beg + (c - cs) * kMsHeavyChunk;
       const uint32_t lab = (uint32_t)key;
-      const uint64_t sub = labels[u];
-      const uint64_t beg = S.off[u], end = S.off[u + 1];
-      bool failed = false;
-      for (uint64_t b = beg + (uint64_t)blockIdx.x * BLOCK + wid * 32; b < end; b += stride) {
-        const uint64_t e = b + lane;
-        bool take = false;
-        uint64_t nk = 0;
+      uint32_t w[K];
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const uint64_t e = e0 + k * 32 + lane;
+        w[k] = 0xFFFFFFFFu;
         if (e < end) {
           scanned++;
-          const uint32_t w = __ldg(&S.E[e]);
-          if (__ldg(&labels[w]) == sub) {
-            nk = ((uint64_t)w << 32) | lab;
-            int r = table_insert(S.T, S.mask, nk, kProbeLimit, &probes);
-            take = r == 1;
-            failed |= r < 0;
-          }
+          w[k] = __ldg(&S.E[e]);
         }
-        ins += take ? 1 : 0;
-        unsigned long long pos = warp_append(&S.ctr->next, take);
-        if (take) S.Fout[pos] = nk;
       }
-      // one re-queue per heavy pair, whichever warp saw the failure first
+      uint64_t nk[K];
+      uint32_t tm = 0;
+      bool failed = false;
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        nk[k] = 0;
+        if (w[k] != 0xFFFFFFFFu && __ldg(&labels[w[k]]) == sub) {
+          nk[k] = ((uint64_t)w[k] << 32) | lab;
+          const int r = table_insert(S.T, S.mask, nk[k], kProbeLimit, &probes);
+          if (r == 1) tm |= 1u << k;
+          failed |= r < 0;
+        }
+      }
+      ins += __popc(tm);
+      warp_append_batch<K>(tm, nk, S.Fout, &S.ctr->next);
       bool rq = false;
-      if (__any_sync(kFull, failed) && lane == 0) rq = atomicExch(&S.hflag[hh], 1u) == 0;
-      unsigned long long pos = warp_append(&S.ctr->next, rq);
+      if (__any_sync(kFull, failed) && lane == 0)
+        rq = !(atomicOr(&S.hflag[h], kRequeued) & kRequeued);
+      const unsigned long long pos = warp_append(&S.ctr->next, rq);
       if (rq) {
         S.Fout[pos] = key;
         requeued++;
@@ -626,7 +671,7 @@ __global__ void __launch_bounds__(BLOCK)
     scanned = warp_sum(scanned);
     requeued = warp_sum(requeued);
     ins = warp_sum(ins);
-    unsigned long long pr = warp_sum((unsigned long long)probes);
+    const unsigned long long pr = warp_sum((unsigned long long)probes);
     if (lane == 0) {
       if (ins) atomicAdd(&S.ctr->inserted, ins);
       if (scanned) atomicAdd(&S.ctr->heavy_edges, scanned);
@@ -700,6 +745,8 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
 int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t label_offset,
             const uint64_t* labels, const psc_params_t* p, const uint64_t prev_ne[2],
             MsResult out[2], const uint32_t* front_labels, uint64_t vgc_max) {
+  // heavy-list fields: < 2^24 pairs (m / kHeavyDeg), first chunks < 2^31
+  if (g->m >> 36) return PSC_ERR_TOO_LARGE;
   const uint32_t tau = p->tau ? p->tau : 512;
   const bool local = p->local_scc != 0;
   const uint64_t vgc_limit = vgc_max ? vgc_max : (uint64_t)g->num_sms * 32;
@@ -815,7 +862,8 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
         for (int k = 0; k < 2; k++)
           if (st[k].nf) {
             const Counters& c = g->hctr[st[k].cset];
-            g->prof[F_HEAVY].bytes += 24.0 * c.heavy + 12.0 * c.heavy_edges + 8.0 * c.heavy_probes;
+            g->prof[F_HEAVY].bytes +=
+                28.0 * (c.heavy >> kPackShift) + 12.0 * c.heavy_edges + 8.0 * c.heavy_probes;
           }
     }
     if (trace_on()) {

@@ -36,6 +36,8 @@ constexpr int kVgcBlock = 128;  // VGC blocks: 4 warps
 constexpr int kVgcQueue = 512;  // VGC queue entries per warp (8 KB of 16-byte entries)
 constexpr int kExpandK = 8;     // VGC: edges in flight per lane
 constexpr int kPushK = 4;       // push: edges in flight per lane
+constexpr int kHeavyK = 4;      // heavy vertices: edges in flight per lane
+constexpr uint64_t kHeavyChunk = 32 * kHeavyK;  // edges of one heavy-list work unit
 
 // One search side as the kernels see it.
 struct ReachSide {
@@ -45,9 +47,19 @@ struct ReachSide {
   uint64_t nin;
   uint32_t* vis;        // visited bitmap
   uint32_t* qout;       // next frontier (queue)
-  uint32_t* heavy;      // heavy list
+  uint64_t* heavy;      // heavy list: vertex << 32 | first chunk (see heavy_push)
   Counters* ctr;
 };
+
+// Lists a vertex with more than kHeavyDeg out-edges for k_reach_heavy.  Its
+// edges are cut into chunks of kHeavyChunk; one 64-bit atomic on ctr->heavy =
+// count << kPackShift | chunks gives the entry its slot and its first chunk,
+// so entries in slot order have increasing first chunks.
+__device__ __forceinline__ void heavy_push(const ReachSide& S, uint32_t u, uint64_t deg) {
+  const unsigned long long old = atomicAdd(
+      &S.ctr->heavy, (1ull << kPackShift) + (deg + kHeavyChunk - 1) / kHeavyChunk);
+  S.heavy[old >> kPackShift] = ((uint64_t)u << 32) | (old & kPackMask);
+}
 
 __global__ void k_reach_init(uint32_t* vis, uint32_t* q, uint32_t src) {
   vis[src >> 5] = 1u << (src & 31);
@@ -167,7 +179,7 @@ __global__ void __launch_bounds__(BLOCK) k_reach_push(ReachSide s0, ReachSide s1
       uint64_t d = S.off[u + 1] - beg;
       (sd ? exp1 : exp0)++;
       if (d > kHeavyDeg) {
-        S.heavy[atomicAdd(&S.ctr->heavy, 1ull)] = u;
+        heavy_push(S, u, d);
         d = 0;
       }
       deg = (uint32_t)d;
@@ -317,7 +329,7 @@ __global__ void __launch_bounds__(BLOCK)
       ub = S.off[u];
       du = S.off[u + 1] - ub;
       (sd ? exp1 : exp0)++;
-      if (du > kHeavyDeg) S.heavy[atomicAdd(&S.ctr->heavy, 1ull)] = u;
+      if (du > kHeavyDeg) heavy_push(S, u, du);
     }
     uint32_t big = __ballot_sync(kFull, lane < cnt && du >= tq && du <= kHeavyDeg);
     while (big) {
@@ -409,36 +421,63 @@ __global__ void __launch_bounds__(BLOCK)
   flush_side_counters(s0.ctr, s1.ctr, scanned0, scanned1, nedges0, nedges1, exp0, exp1);
 }
 
-// The whole grid walks the edges of every heavy vertex of both sides, 32
-// edges per warp step.
+// Heavy vertices of both sides: the chunks of a side's heavy list are cut
+// into one contiguous range per warp; a warp finds the entry of its first
+// chunk once, then claims kHeavyChunk edges per step (a heavy vertex has
+// more than 64 chunks, so the next entry is at most one step away).
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_reach_heavy(ReachSide s0, ReachSide s1) {
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const uint64_t stride = (uint64_t)gridDim.x * BLOCK;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
 #pragma unroll 1
   for (int sd = 0; sd < 2; sd++) {
     const ReachSide S = sd ? s1 : s0;
     if (!S.ctr) continue;
-    const uint64_t nh = *(volatile unsigned long long*)&S.ctr->heavy;
+    const unsigned long long packed = S.ctr->heavy;
+    const uint64_t nh = packed >> kPackShift, total = packed & kPackMask;
+    const uint64_t per = (total + nw - 1) / nw;
+    const uint64_t c_beg = gw * per, c_end = c_beg + per < total ? c_beg + per : total;
+    if (nh == 0 || c_beg >= c_end) continue;
+    uint64_t h = 0, hi = nh - 1;  // last entry whose first chunk is <= c_beg
+    while (h < hi) {
+      const uint64_t mid = (h + hi + 1) >> 1;
+      if ((uint32_t)__ldg(&S.heavy[mid]) <= c_beg)
+        h = mid;
+      else
+        hi = mid - 1;
+    }
+    uint64_t ent = __ldg(&S.heavy[h]);
+    uint64_t cs = (uint32_t)ent, cn = h + 1 < nh ? (uint32_t)__ldg(&S.heavy[h + 1]) : total;
+    uint64_t beg = S.off[ent >> 32], end = S.off[(ent >> 32) + 1];
     unsigned long long scanned = 0, next_edges = 0;
-    for (uint64_t h = 0; h < nh; h++) {
-      const uint32_t u = S.heavy[h];
-      const uint64_t beg = S.off[u], end = S.off[u + 1];
-      for (uint64_t b = beg + (uint64_t)blockIdx.x * BLOCK + wid * 32; b < end; b += stride) {
-        const uint64_t e = b + lane;
-        uint32_t v = 0;
-        bool take = false;
+    for (uint64_t c = c_beg; c < c_end; c++) {
+      if (c >= cn) {
+        h++;
+        ent = __ldg(&S.heavy[h]);
+        cs = cn;
+        cn = h + 1 < nh ? (uint32_t)__ldg(&S.heavy[h + 1]) : total;
+        beg = S.off[ent >> 32];
+        end = S.off[(ent >> 32) + 1];
+      }
+      const uint64_t e0 = beg + (c - cs) * kHeavyChunk;
+      uint32_t v[kHeavyK], tm = 0;
+#pragma unroll
+      for (int k = 0; k < kHeavyK; k++) {
+        const uint64_t e = e0 + k * 32 + lane;
+        v[k] = 0;
         if (e < end) {
           scanned++;
-          v = __ldg(&S.E[e]);
-          take = bit_set(S.vis, v);
-        }
-        unsigned long long pos = warp_append(&S.ctr->next, take);
-        if (take) {
-          S.qout[pos] = v;
-          next_edges += S.off[v + 1] - S.off[v];
+          v[k] = __ldg(&S.E[e]);
         }
       }
+#pragma unroll
+      for (int k = 0; k < kHeavyK; k++)
+        if (e0 + k * 32 + lane < end && bit_set(S.vis, v[k])) tm |= 1u << k;
+      warp_append_batch<kHeavyK>(tm, v, S.qout, &S.ctr->next);
+#pragma unroll
+      for (int k = 0; k < kHeavyK; k++)
+        if (tm & (1u << k)) next_edges += S.off[v[k] + 1] - S.off[v[k]];
     }
     scanned = warp_sum(scanned);
     next_edges = warp_sum(next_edges);
@@ -613,7 +652,7 @@ ReachSide side_args(psc_graph_s* g, const Side& s) {
   r.nin = s.nf;
   r.vis = s.vis;
   r.qout = (uint32_t*)g->bufs[s.slot_qb].p;
-  r.heavy = (uint32_t*)g->bufs[s.slot_heavy].p;
+  r.heavy = (uint64_t*)g->bufs[s.slot_heavy].p;
   r.ctr = g->ctr + s.cset;
   return r;
 }
@@ -640,6 +679,8 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
                        uint32_t tau, uint32_t pull_div, const uint32_t* d_srcs = nullptr,
                        uint64_t n_dsrc = 0, uint64_t vgc_max = 0) {
   const uint64_t n = g->n, nwords = (n + 31) / 32;
+  // heavy-list fields: < 2^24 entries (m / kHeavyDeg), < 2^32 chunks
+  if (g->m >> 36) return PSC_ERR_TOO_LARGE;
   // VGC rounds while the frontier is below one vertex per resident warp
   // (unless the caller sets the limit)
   const uint64_t vgc_limit = vgc_max ? vgc_max : (uint64_t)g->num_sms * 64;
@@ -652,7 +693,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
     PSC_TRY(ensure(g, s.slot_qb, (n + 1) * 4, &p));
     PSC_TRY(ensure(g, s.slot_fa, (nwords + 1) * 4, &p));
     PSC_TRY(ensure(g, s.slot_fb, (nwords + 1) * 4, &p));
-    PSC_TRY(ensure(g, s.slot_heavy, (n + 1) * 4, &p));
+    PSC_TRY(ensure(g, s.slot_heavy, (n + 1) * 8, &p));
     PSC_CUDA(cudaMemsetAsync(s.vis, 0, nwords * 4, g->stream));
     if (d_srcs) {
       if (n_dsrc)
@@ -785,7 +826,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       if (g->profiling)
         for (int k = 0; k < nh; k++) {
           const Counters& c = g->hctr[hv[k].ctr - g->ctr];
-          g->prof[F_HEAVY].bytes += 20.0 * c.heavy + 5.0 * c.heavy_edges;
+          g->prof[F_HEAVY].bytes += 24.0 * (c.heavy >> kPackShift) + 5.0 * c.heavy_edges;
         }
     }
     if (tr) {
@@ -892,8 +933,8 @@ constexpr size_t kNaFa = kNaVis + kNaBitmap;
 constexpr size_t kNaFb = kNaFa + kNaBitmap;
 constexpr size_t kNaQa = kNaFb + kNaBitmap;
 constexpr size_t kNaQb = kNaQa + kNaQueue;
-constexpr size_t kNaHeavy = kNaQb + kNaQueue;
-constexpr size_t kNaCtr = kNaHeavy + kNaQueue;
+constexpr size_t kNaHeavy = kNaQb + kNaQueue;  // u64 entries: two u32 per vertex
+constexpr size_t kNaCtr = kNaHeavy + 2 * kNaQueue;
 constexpr size_t kNaTotal = kNaCtr + 64;
 static_assert(sizeof(Counters) <= 64 * sizeof(uint32_t), "counters fit their region");
 static_assert(kNaCtr % 64 == 0, "256-byte aligned counters");
@@ -943,7 +984,7 @@ extern "C" int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E,
                                  const uint64_t* d_in_off, const uint32_t* d_in_E, uint64_t n,
                                  uint64_t m, uint32_t src, int dir, uint8_t* d_dst, void* stream,
                                  uint32_t* rounds) {
-  if (n > kNaMaxN) return PSC_ERR_TOO_LARGE;
+  if (n > kNaMaxN || (m >> 36)) return PSC_ERR_TOO_LARGE;
   if (!d_off || (m && !d_E) || !d_dst || n == 0 || src >= n || (dir != 0 && dir != 1))
     return PSC_ERR_INVALID;
   if ((d_in_off == nullptr) != (d_in_E == nullptr)) return PSC_ERR_INVALID;
@@ -967,7 +1008,7 @@ extern "C" int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E,
   uint32_t* fb = nd.scratch + kNaFb;
   uint32_t* qa = nd.scratch + kNaQa;
   uint32_t* qb = nd.scratch + kNaQb;
-  uint32_t* heavy = nd.scratch + kNaHeavy;
+  uint64_t* heavy = (uint64_t*)(nd.scratch + kNaHeavy);
   Counters* ctr = (Counters*)(nd.scratch + kNaCtr);
   Counters hc;  // host copy of the counters (stack memory)
 

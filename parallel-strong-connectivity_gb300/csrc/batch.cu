@@ -181,18 +181,29 @@ __global__ void k_batch_sources(const uint32_t* __restrict__ P, const uint64_t* 
     srcs[j] = P[npbase[graphs[j]]];
 }
 
-__global__ void k_label_first_b(const uint32_t* __restrict__ P, uint64_t np,
-                                const uint32_t* __restrict__ vf, const uint32_t* __restrict__ vb,
-                                const uint32_t* __restrict__ gid, const uint64_t* __restrict__ lo,
-                                uint64_t* labels) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t v = P[i];
-    const bool f = (vf[v >> 5] >> (v & 31)) & 1u, b = (vb[v >> 5] >> (v & 31)) & 1u;
-    if (f || b) {
-      const uint64_t label = lo[gid[v]];
-      labels[v] = (f && b) ? (label | kTopBit) : label;
+// First-pivot labels of every graph, in vertex order (see k_label_first):
+// reached vertices that trimming did not finish take their graph's label;
+// the bitmap of finished vertices is written alongside.
+__global__ void k_label_first_b(const uint32_t* __restrict__ vf, const uint32_t* __restrict__ vb,
+                                uint64_t n, const uint32_t* __restrict__ gid,
+                                const uint64_t* __restrict__ lo, uint64_t* labels, uint32_t* done) {
+  const unsigned lane = lane_id();
+  for (uint64_t base = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ull; base < n;
+       base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v = base + lane;
+    bool fin = false;
+    if (v < n) {
+      const uint32_t bit = 1u << lane;
+      const bool f = __ldg(&vf[base >> 5]) & bit, b = __ldg(&vb[base >> 5]) & bit;
+      fin = labels[v] & kTopBit;
+      if ((f || b) && !fin) {
+        const uint64_t label = lo[gid[v]];
+        labels[v] = (f && b) ? (label | kTopBit) : label;
+        fin = f && b;
+      }
     }
+    const uint32_t word = __ballot_sync(kFull, fin);
+    if (lane == 0) done[base >> 5] = word;
   }
 }
 
@@ -393,10 +404,13 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
     PSC_TRY(reach_pair_multi(g, A.srcs, ns, p->local_reach != 0, p->tau, p->pull_div, vf, vb, &r1,
                              &r2, kBatchVgcMax));
     g->stats.reach_rounds = r1 + r2;
+    uint32_t* done;  // finished vertices after the first pivots (frontier slot, free by now)
+    PSC_TRY(ensure_t(g, B_FB_A, (n + 31) / 32 + 1, &done));
     {
       ProfScope ps(g, F_LABEL_FIRST);
-      ps.bytes = 4.0 * np + 12.0 * np;
-      k_label_first_b<<<grid_for(g, np, tb), tb, 0, g->stream>>>(P, np, vf, vb, gid, A.lo, labels);
+      ps.bytes = 0.375 * g->n + 8.0 * g->n + 12.0 * np;
+      k_label_first_b<<<grid_for(g, g->n, tb), tb, 0, g->stream>>>(vf, vb, g->n, gid, A.lo, labels,
+                                                                 done);
     }
     {
       ProfScope ps(g, F_BATCH);
@@ -404,7 +418,8 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
     }
     PSC_TRY(ensure_t(g, B_CENTERS, np + 1, &centres));
     uint64_t nc = 0;
-    PSC_TRY(scan_emit(g, np, NotDoneAt{P, labels, 0}, CopyAt{P, centres, 0}, &nc, F_COMPACT, 12.0, 4.0));
+    PSC_TRY(scan_emit(g, np, NotDoneBitAt{P, done}, CopyAt{P, centres, 0}, &nc, F_COMPACT, 8.0,
+                      4.0));
     {
       ProfScope ps(g, F_BATCH);
       k_bases_by_graph<<<(G + 256) / 256, 256, 0, g->stream>>>(centres, nc, gid, nullptr, G, A.cbase);

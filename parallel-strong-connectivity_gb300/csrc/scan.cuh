@@ -133,6 +133,16 @@ struct NotDoneAt {
   }
 };
 
+// Not done according to a bitmap of finished vertices (see k_label_first).
+struct NotDoneBitAt {
+  const uint32_t* src;
+  const uint32_t* done;
+  __device__ uint32_t operator()(uint64_t i) const {
+    const uint32_t v = src[i];
+    return ((__ldg(&done[v >> 5]) >> (v & 31)) & 1u) ^ 1u;
+  }
+};
+
 struct CopyAt {
   const uint32_t* src;
   uint32_t* dst;

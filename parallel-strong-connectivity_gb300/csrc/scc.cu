@@ -49,17 +49,29 @@ __global__ void k_perm_gather(const uint32_t* __restrict__ nz, uint64_t np, Feis
     P[i] = nz[feistel(key, i)];
 }
 
-__global__ void k_label_first(const uint32_t* __restrict__ P, uint64_t np,
-                              const uint32_t* __restrict__ vf, const uint32_t* __restrict__ vb,
-                              uint64_t* labels, uint64_t label) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t v = P[i];
-    bool f = (vf[v >> 5] >> (v & 31)) & 1u, b = (vb[v >> 5] >> (v & 31)) & 1u;
-    if (f && b)
-      labels[v] = label | kTopBit;
-    else if (f || b)
-      labels[v] = label;
+// First-pivot labels (scc.hpp:340-349) in vertex order: a warp reads one word
+// of each bitmap for its 32 vertices and writes the labels of reached vertices
+// that trimming did not finish (labels without kTopBit).  It also writes the
+// bitmap of finished vertices (trimmed, or reached both ways), one ballot per
+// 32 vertices, for the compaction of the pivot order that follows.
+__global__ void k_label_first(const uint32_t* __restrict__ vf, const uint32_t* __restrict__ vb,
+                              uint64_t n, uint64_t* labels, uint64_t label, uint32_t* done) {
+  const unsigned lane = lane_id();
+  for (uint64_t base = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ull; base < n;
+       base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v = base + lane;
+    bool fin = false;
+    if (v < n) {
+      const uint32_t bit = 1u << lane;
+      const bool f = __ldg(&vf[base >> 5]) & bit, b = __ldg(&vb[base >> 5]) & bit;
+      fin = labels[v] & kTopBit;
+      if ((f || b) && !fin) {
+        labels[v] = (f && b) ? (label | kTopBit) : label;
+        fin = f && b;
+      }
+    }
+    const uint32_t word = __ballot_sync(kFull, fin);
+    if (lane == 0) done[base >> 5] = word;
   }
 }
 
@@ -185,14 +197,19 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
     uint32_t r1 = 0, r2 = 0;
     PSC_TRY(reach_pair(g, src, p->local_reach != 0, p->tau, p->pull_div, vf, vb, &r1, &r2));
     g->stats.reach_rounds = r1 + r2;
+    uint32_t* done;  // finished vertices after the first pivot (frontier slot, free by now)
+    PSC_TRY(ensure_t(g, B_FB_A, (n + 31) / 32 + 1, &done));
     {
       ProfScope ps(g, F_LABEL_FIRST);
-      ps.bytes = 4.0 * np + 8.0 * np;
-      k_label_first<<<grid_for(g, np, tb), tb, 0, g->stream>>>(P, np, vf, vb, labels, label_offset);
+      // two bitmaps read and one written; label read per vertex, written per live vertex
+      ps.bytes = 0.375 * n + 8.0 * n + 8.0 * np;
+      k_label_first<<<grid_for(g, n, tb), tb, 0, g->stream>>>(vf, vb, n, labels, label_offset,
+                                                            done);
     }
     PSC_TRY(ensure_t(g, B_CENTERS, np + 1, &centers));
     uint64_t nc = 0;
-    PSC_TRY(scan_emit(g, np, NotDoneAt{P, labels, 0}, CopyAt{P, centers, 0}, &nc, F_COMPACT, 12.0, 4.0));
+    PSC_TRY(scan_emit(g, np, NotDoneBitAt{P, done}, CopyAt{P, centers, 0}, &nc, F_COMPACT, 8.0,
+                      4.0));
     label_offset++;
     PSC_CUDA(cudaEventRecord(g->ph[2], g->stream));
 

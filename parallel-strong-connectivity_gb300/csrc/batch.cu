@@ -359,7 +359,8 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
 
   // trim over the union
   uint64_t n_zeros = 0;
-  PSC_TRY(scan_emit(g, n, ZeroFlag{g->off, g->in_off}, TrimEmitB{labels, nz}, &n_zeros, F_TRIM, 40.0));
+  PSC_TRY(scan_emit_flags(g, n, ZeroFlag{g->off, g->in_off}, TrimEmitB{labels, nz}, &n_zeros, F_TRIM,
+                          28.0));
   const uint64_t np = n - n_zeros;
   std::vector<uint64_t> npbase(G + 1), cbase(G + 1);
   {
@@ -418,7 +419,7 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
     }
     PSC_TRY(ensure_t(g, B_CENTERS, np + 1, &centres));
     uint64_t nc = 0;
-    PSC_TRY(scan_emit(g, np, NotDoneBitAt{P, done}, CopyAt{P, centres, 0}, &nc, F_COMPACT, 8.0,
+    PSC_TRY(scan_emit_flags(g, np, NotDoneBitAt{P, done}, CopyAt{P, centres, 0}, &nc, F_COMPACT, 8.0,
                       4.0));
     {
       ProfScope ps(g, F_BATCH);
@@ -469,7 +470,7 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
       const uint64_t W = hs[at[j] + 3 * c];
       const WinNotDone wnd{centres, labels, wstart, wpre, c};
       uint64_t nf = 0;
-      PSC_TRY(scan_emit(g, W, wnd, WinCopy{wnd, front}, &nf, F_COMPACT, 12.0, 4.0));
+      PSC_TRY(scan_emit_flags(g, W, wnd, WinCopy{wnd, front}, &nf, F_COMPACT, 12.0, 4.0));
       if (nf == 0) continue;
       g->stats.batches++;
       {

@@ -175,6 +175,7 @@ enum Buf : int {
   B_GRAPHS,       // per-graph arrays of a batch
   B_FLAB,         // u32 labels of a batch's pivots
   B_SCHED,        // window schedule of a batch's prefix-doubling rounds
+  B_SCANBITS,     // u32[n/32] selection bits of scan_emit_flags
   B_COUNT
 };
 

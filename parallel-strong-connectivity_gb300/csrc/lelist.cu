@@ -980,7 +980,8 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   uint32_t* out;
   PSC_TRY(ensure_t(g, B_AUX0, 3 * L + 3, &out));
   uint64_t kept = 0;
-  PSC_TRY(scan_emit(g, L, KeepValue{keep}, TripleEmit{Bk, tgt, centers, out}, &kept, F_LE_SORT));
+  PSC_TRY(scan_emit_flags(g, L, KeepValue{keep}, TripleEmit{Bk, tgt, centers, out}, &kept,
+                          F_LE_SORT));
   *len_out = kept;
   return PSC_OK;
 }

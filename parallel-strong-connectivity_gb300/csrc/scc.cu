@@ -175,8 +175,10 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
   PSC_TRY(ensure_t(g, B_TMP32, n + 1, &nz));
   // trim
   uint64_t n_zeros = 0;
-  // algorithmic bytes: 4 offsets read + one 8-byte label or 4-byte index written
-  PSC_TRY(scan_emit(g, n, ZeroFlag{g->off, g->in_off}, TrimEmit{labels, nz}, &n_zeros, F_TRIM, 40.0));
+  // algorithmic bytes: two offsets of each direction read, an 8-byte label and
+  // (for the live vertices) a 4-byte index written
+  PSC_TRY(scan_emit_flags(g, n, ZeroFlag{g->off, g->in_off}, TrimEmit{labels, nz}, &n_zeros, F_TRIM,
+                          28.0));
   const uint64_t np = n - n_zeros;
   if (np > 0) {
     FeistelKey key = feistel_key(np, p->seed);
@@ -208,7 +210,7 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
     }
     PSC_TRY(ensure_t(g, B_CENTERS, np + 1, &centers));
     uint64_t nc = 0;
-    PSC_TRY(scan_emit(g, np, NotDoneBitAt{P, done}, CopyAt{P, centers, 0}, &nc, F_COMPACT, 8.0,
+    PSC_TRY(scan_emit_flags(g, np, NotDoneBitAt{P, done}, CopyAt{P, centers, 0}, &nc, F_COMPACT, 8.0,
                       4.0));
     label_offset++;
     PSC_CUDA(cudaEventRecord(g->ph[2], g->stream));
@@ -226,7 +228,7 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
       if (step_size > n_remaining) step_size = n_remaining;
       if (step_size == 0) step_size = 1;
       uint64_t nf = 0;
-      PSC_TRY(scan_emit(g, vs_size, NotDoneAt{centers, labels, cur_offset},
+      PSC_TRY(scan_emit_flags(g, vs_size, NotDoneAt{centers, labels, cur_offset},
                         CopyAt{centers, front, cur_offset}, &nf, F_COMPACT, 12.0, 4.0));
       cur_offset = end;
       if (nf == 0) continue;

@@ -74,7 +74,9 @@ struct Counters {
   unsigned long long waves;        // local-search waves of VGC rounds (trace)
   unsigned long long pad[2];
 };
-constexpr int kCounterSets = 4;
+// sets 0-1: search sides; 2-3: staging; 4-19: the rounds of a chained VGC
+// sequence (reach.cu), two sides per round
+constexpr int kCounterSets = 20;
 
 // ---------------------------------------------------------------------------
 // Host-side helpers
@@ -112,6 +114,8 @@ struct psc_graph_s {
   int ms_vgc_blocks = 0;  // same for the multi-search VGC kernel
   int ldd_vgc_blocks = 0; // same for the LDD VGC kernel
   int le_heavy_blocks = 0; // same for the LE-list heavy-pair kernel
+  bool deg_known = false;    // max_deg holds the largest out- / in-degree
+  uint64_t max_deg[2] = {0, 0};
   uint32_t block = 0;     // threads per block of the expansion kernels (0: 256)
   // named scratch buffers, grown on demand (stream-ordered allocator)
   std::vector<psc::DevBuf> bufs;

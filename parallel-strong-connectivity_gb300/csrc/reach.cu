@@ -49,6 +49,9 @@ struct ReachSide {
   uint32_t* qout;       // next frontier (queue)
   uint64_t* heavy;      // heavy list: vertex << 32 | first chunk (see heavy_push)
   Counters* ctr;
+  // chained VGC rounds: when set, the frontier size is read here (the
+  // previous round's ctr->next) instead of nin
+  const unsigned long long* nin_dev;
 };
 
 // Lists a vertex with more than kHeavyDeg out-edges for k_reach_heavy.  Its
@@ -309,6 +312,12 @@ __global__ void __launch_bounds__(BLOCK)
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  if (s0.nin_dev) s0.nin = *s0.nin_dev;
+  if (s1.nin_dev) s1.nin = *s1.nin_dev;
+  if (chunk == 0) {  // chained round: chunk size from the device frontier sizes
+    const uint64_t per = (s0.nin + s1.nin + nw - 1) / nw;
+    chunk = (uint32_t)(per < 1 ? 1 : per > 32 ? 32 : per);
+  }
   const uint32_t tq = tau < (uint32_t)QCAP ? tau : (uint32_t)QCAP;
   // A round lasts as long as its longest local search.  Searches that stay
   // narrow (a few vertices per wave) stop after max_waves waves and spill
@@ -639,15 +648,59 @@ __global__ void k_bitmap_to_bytes(const uint32_t* __restrict__ vis, uint64_t n, 
 // ---------------------------------------------------------------------------
 namespace {
 
+// Largest out-degree (out[0]) and in-degree (out[1]) of the graph.
+__global__ void k_max_degrees(const uint64_t* __restrict__ off, const uint64_t* __restrict__ in_off,
+                              uint64_t n, unsigned long long* out) {
+  unsigned long long a = 0, b = 0;
+  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned long long x = off[v + 1] - off[v], y = in_off[v + 1] - in_off[v];
+    a = x > a ? x : a;
+    b = y > b ? y : b;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(kFull, a, o), y = __shfl_xor_sync(kFull, b, o);
+    a = x > a ? x : a;
+    b = y > b ? y : b;
+  }
+  if (lane_id() == 0) {
+    if (a) atomicMax(&out[0], a);
+    if (b) atomicMax(&out[1], b);
+  }
+}
+
+// Once per handle (the graph does not change): max_deg for the heavy-vertex
+// check of chained rounds.
+static int ensure_max_degrees(psc_graph_s* g) {
+  if (g->deg_known) return PSC_OK;
+  unsigned long long* d = &g->ctr[2].aux0;  // aux0, aux1 of the staging set
+  PSC_CUDA(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), g->stream));
+  k_max_degrees<<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(g->off, g->in_off, g->n, d);
+  PSC_CUDA(cudaGetLastError());
+  PSC_TRY(read_counters(g));
+  g->max_deg[0] = g->hctr[2].aux0;
+  g->max_deg[1] = g->hctr[2].aux1;
+  g->deg_known = true;
+  return PSC_OK;
+}
+
 struct Side {
   bool backward = false;
   uint32_t* vis = nullptr;
   int slot_qa = 0, slot_qb = 0, slot_fa = 0, slot_fb = 0, slot_heavy = 0;
   int cset = 0;  // counter block
-  uint64_t nf = 0, nf_edges = 0;
+  uint64_t nf = 0, nf_edges = 0, prev_nf = 0;
   bool pull = false;
   uint32_t rounds = 0;
 };
+
+// Chained VGC rounds (see reach_sides): rounds per chain, and the counter set
+// of side k in round j of a chain.
+constexpr int kVgcChain = 8;
+static_assert(kVgcChain % 2 == 0, "a chain leaves the frontier in the side's first queue");
+constexpr int chain_set(int j, int k) { return 4 + 2 * j + k; }
+static_assert(chain_set(kVgcChain - 1, 1) < kCounterSets, "chain counter sets");
 
 enum Mode { M_NONE, M_VGC, M_PUSH, M_PULL };
 
@@ -661,6 +714,7 @@ ReachSide side_args(psc_graph_s* g, const Side& s) {
   r.qout = (uint32_t*)g->bufs[s.slot_qb].p;
   r.heavy = (uint64_t*)g->bufs[s.slot_heavy].p;
   r.ctr = g->ctr + s.cset;
+  r.nin_dev = nullptr;
   return r;
 }
 
@@ -712,11 +766,103 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       s.nf = 1;
     }
     s.nf_edges = 0;
+    s.prev_nf = 0;
     s.pull = false;
     s.rounds = 0;
   }
+  const bool tr = trace_on();
   for (uint64_t iter = 0;; iter++) {
     if (iter > n + 2) return PSC_ERR_ITER_LIMIT;
+    // Chained VGC rounds: while every active side has a steady frontier well
+    // inside VGC range (at least two rounds done, grown at most 1.5x in the
+    // last one, far from the pull threshold), kVgcChain rounds are launched
+    // back to back, each reading its frontier size from the previous round's
+    // counters on the device, and the counters are read back once for the
+    // whole chain instead of once per round.  Every round is a VGC round as
+    // the switch would have chosen it; a round of a side that ran dry does
+    // nothing.
+    if (local) {
+      int act[2], na = 0;
+      bool steady = true;
+      for (int k = 0; k < ns; k++) {
+        const Side& s = sides[k];
+        if (s.nf == 0) continue;
+        act[na++] = k;
+        steady = steady && !s.pull && s.rounds >= 2 && s.nf <= vgc_limit &&
+                 2 * s.nf <= 3 * s.prev_nf && 3 * (s.nf + s.nf_edges) < threshold;
+      }
+      if (na > 0 && steady) {
+        PSC_TRY(ensure_max_degrees(g));
+        bool heavy_possible = false;  // some active direction has a vertex above kHeavyDeg
+        for (int a = 0; a < na; a++)
+          heavy_possible |= g->max_deg[sides[act[a]].backward ? 1 : 0] > kHeavyDeg;
+        if (!g->vgc_blocks) {
+          PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue>, kVgcBlock, 0));
+          if (g->vgc_blocks < 1) g->vgc_blocks = 1;
+        }
+        const unsigned blocks = (unsigned)((uint64_t)g->num_sms * g->vgc_blocks);
+        PSC_TRY(zero_counters(g));
+        for (int j = 0; j < kVgcChain; j++) {
+          ReachSide vg[2] = {};
+          for (int a = 0; a < na; a++) {
+            const Side& s = sides[act[a]];
+            ReachSide r = side_args(g, s);
+            uint32_t* qa = (uint32_t*)g->bufs[s.slot_qa].p;
+            uint32_t* qb = (uint32_t*)g->bufs[s.slot_qb].p;
+            r.qin = (j & 1) ? qb : qa;
+            r.qout = (j & 1) ? qa : qb;
+            r.ctr = g->ctr + chain_set(j, a);
+            r.nin_dev = j ? &g->ctr[chain_set(j - 1, a)].next : nullptr;
+            vg[a] = r;
+          }
+          {
+            ProfScope ps(g, F_REACH_VGC);
+            k_reach_vgc<kVgcBlock, kVgcQueue><<<blocks, kVgcBlock, 0, g->stream>>>(vg[0], vg[1],
+                                                                                 tau, 0u);
+          }
+          if (heavy_possible) {
+            // heavy vertices queued by this round (the kernel returns at once
+            // when there are none)
+            ProfScope ps(g, F_HEAVY);
+            k_reach_heavy<kReachBlock><<<g->num_sms * 4, kReachBlock, 0, g->stream>>>(vg[0], vg[1]);
+          }
+        }
+        PSC_CUDA(cudaGetLastError());
+        PSC_TRY(read_counters(g));
+        float t_ms = 0;
+        if (tr) {
+          cudaEvent_t e = take_event(g);
+          PSC_CUDA(cudaEventRecord(e, g->stream));
+          PSC_CUDA(cudaEventSynchronize(e));
+          cudaEventElapsedTime(&t_ms, g->t0, e);
+          give_event(g, e);
+        }
+        for (int a = 0; a < na; a++) {
+          Side& s = sides[act[a]];
+          uint64_t nin = s.nf;
+          for (int j = 0; j < kVgcChain && nin; j++) {
+            const Counters& c = g->hctr[chain_set(j, a)];
+            s.rounds++;
+            if (g->profiling) {
+              g->prof[F_REACH_VGC].bytes += 16.0 * c.expanded + 5.0 * c.edges + 5.0 * c.next;
+              g->prof[F_HEAVY].bytes += 24.0 * (c.heavy >> kPackShift) + 5.0 * c.heavy_edges;
+            }
+            if (tr)
+              std::fprintf(stderr, "reach side %d round %u mode vgc-chain nf %llu next %llu edges %llu "
+                           "expanded %llu waves %llu t %.3f ms\n",
+                           act[a], s.rounds, (unsigned long long)nin, c.next, c.edges, c.expanded,
+                           c.waves, t_ms);
+            s.prev_nf = nin;
+            nin = c.next;
+          }
+          const Counters& last = g->hctr[chain_set(kVgcChain - 1, a)];
+          s.nf = last.next;  // zero when the side ran dry inside the chain
+          s.nf_edges = last.next_edges;
+        }
+        continue;
+      }
+    }
     Mode mode[2] = {M_NONE, M_NONE};
     bool any = false;
     for (int k = 0; k < ns; k++) {
@@ -813,7 +959,6 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
     }
     PSC_CUDA(cudaGetLastError());
     cudaEvent_t tr_b = nullptr;
-    const bool tr = trace_on();
     if (tr) {
       tr_b = take_event(g);
       PSC_CUDA(cudaEventRecord(tr_b, g->stream));
@@ -867,6 +1012,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
         std::swap(g->bufs[s.slot_fa], g->bufs[s.slot_fb]);
       else
         std::swap(g->bufs[s.slot_qa], g->bufs[s.slot_qb]);
+      s.prev_nf = s.nf;
       s.nf = c.next;
       s.nf_edges = c.next_edges;
     }

@@ -726,7 +726,7 @@ def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
 
 # DRAM bytes (read + write) of one launch of a workload's dominant kernel from
 # one ncu capture of the same command (profiles/k_reach_vgc_knn1e7.md).
-NCU_TRAFFIC = {("scc_knn", "reach_vgc"): 103.0e6}
+NCU_TRAFFIC = {("scc_knn", "reach_vgc"): 91.9e6}
 
 
 def roofline_of(prof: dict, steps: int, workload: str = "") -> dict:

@@ -34,7 +34,13 @@ namespace psc {
 constexpr int kReachBlock = 256;
 constexpr int kVgcBlock = 128;  // VGC blocks: 4 warps
 constexpr int kVgcQueue = 512;  // VGC queue entries per warp (8 KB of 16-byte entries)
-constexpr int kExpandK = 8;     // VGC: edges in flight per lane
+// VGC: edges in flight per lane.  Sparse graphs (fewer than 8 edges per vertex
+// on average) use 4: fewer registers, 6 instead of 5 resident blocks per SM,
+// more local searches at once (kNN 10^7: 16.8 -> 16.3 ms, grid 4096^2:
+// 17.6 -> 16.3 ms); denser ones and batches use 8 (a 1024-graph batch: 16.2
+// instead of 19.1 ms).
+constexpr int kVgcKWide = 8;
+constexpr int kVgcKNarrow = 4;
 constexpr int kPushK = 4;       // push: edges in flight per lane
 constexpr int kHeavyK = 4;      // heavy vertices: edges in flight per lane
 constexpr uint64_t kHeavyChunk = 32 * kHeavyK;  // edges of one heavy-list work unit
@@ -270,26 +276,27 @@ __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, u
 }
 
 // A frontier vertex with tau..kHeavyDeg out-edges: the warp walks them with
-// kExpandK edges per lane in flight.
+// K edges per lane in flight.
+template <int K>
 __device__ __forceinline__ void vgc_direct(const ReachSide& S, uint64_t ub, uint64_t du,
                                            unsigned long long& nedges) {
   const unsigned lane = lane_id();
   const uint64_t ue = ub + du;
-  for (uint64_t b = ub; b < ue; b += 32 * kExpandK) {
-    uint32_t v[kExpandK];
+  for (uint64_t b = ub; b < ue; b += 32 * K) {
+    uint32_t v[K];
 #pragma unroll
-    for (int k = 0; k < kExpandK; k++) {
+    for (int k = 0; k < K; k++) {
       const uint64_t e = b + k * 32 + lane;
       v[k] = e < ue ? __ldg(&S.E[e]) : 0xFFFFFFFFu;
     }
     uint32_t tm = 0;
 #pragma unroll
-    for (int k = 0; k < kExpandK; k++)
+    for (int k = 0; k < K; k++)
       if (v[k] != 0xFFFFFFFFu && bit_set(S.vis, v[k])) tm |= 1u << k;
 #pragma unroll
-    for (int k = 0; k < kExpandK; k++)
+    for (int k = 0; k < K; k++)
       if (tm & (1u << k)) nedges += S.off[v[k] + 1] - S.off[v[k]];
-    warp_append_batch<kExpandK>(tm, v, S.qout, &S.ctr->next);
+    warp_append_batch<K>(tm, v, S.qout, &S.ctr->next);
   }
 }
 
@@ -304,7 +311,7 @@ __device__ __forceinline__ void vgc_direct(const ReachSide& S, uint64_t ub, uint
 // out-edges, and whatever is left in the queue when it fills or after
 // max_waves waves, are spilled too.
 // Other chunk vertices are expanded directly (heavy ones by the whole grid).
-template <int BLOCK, int QCAP>
+template <int BLOCK, int QCAP, int K>
 __global__ void __launch_bounds__(BLOCK)
     k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau, uint32_t chunk) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
@@ -353,7 +360,7 @@ __global__ void __launch_bounds__(BLOCK)
       big &= big - 1;
       const uint64_t bb = __shfl_sync(kFull, ub, l), bd = __shfl_sync(kFull, du, l);
       if (lane == 0) (sd ? scanned1 : scanned0) += bd;
-      vgc_direct(S, bb, bd, nedges);
+      vgc_direct<K>(S, bb, bd, nedges);
     }
     const bool seed = lane < cnt && du > 0 && du < tq;
     const uint32_t smask = __ballot_sync(kFull, seed);
@@ -400,11 +407,11 @@ __global__ void __launch_bounds__(BLOCK)
       sm[wid].excl[lane] = incl - deg;
       sm[wid].beg[lane] = beg;
       __syncwarp();
-      for (uint32_t base = 0; base < total; base += 32 * kExpandK) {
-        uint32_t w[kExpandK];
-        uint64_t vb[kExpandK], ve[kExpandK];
+      for (uint32_t base = 0; base < total; base += 32 * K) {
+        uint32_t w[K];
+        uint64_t vb[K], ve[K];
 #pragma unroll
-        for (int k = 0; k < kExpandK; k++) {
+        for (int k = 0; k < K; k++) {
           const uint32_t gi = base + k * 32 + lane;
           w[k] = 0xFFFFFFFFu;
           if (gi < total) {
@@ -412,8 +419,8 @@ __global__ void __launch_bounds__(BLOCK)
             w[k] = __ldg(&S.E[sm[wid].beg[src] + (gi - sm[wid].excl[src])]);
           }
         }
-        const uint32_t tm = vgc_claim<kExpandK>(w, vb, ve, S.off, S.vis);
-        vgc_place<kExpandK>(tm, w, vb, ve, Q, tail, tq, S.qout, &S.ctr->next, nedges);
+        const uint32_t tm = vgc_claim<K>(w, vb, ve, S.off, S.vis);
+        vgc_place<K>(tm, w, vb, ve, Q, tail, tq, S.qout, &S.ctr->next, nedges);
       }
     }
     // spill what is left in the queue with one reservation
@@ -648,6 +655,33 @@ __global__ void k_bitmap_to_bytes(const uint32_t* __restrict__ vis, uint64_t n, 
 // ---------------------------------------------------------------------------
 namespace {
 
+// The VGC kernel of a graph (see kVgcKNarrow): its resident blocks per SM
+// (cached on the handle) and its launch.
+static bool vgc_narrow(const psc_graph_s* g) { return g->m < 8 * g->n; }
+
+static int vgc_occupancy(psc_graph_s* g) {
+  if (!g->vgc_blocks) {
+    PSC_CUDA(vgc_narrow(g) ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                 &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow>,
+                                 kVgcBlock, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                 &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide>,
+                                 kVgcBlock, 0));
+    if (g->vgc_blocks < 1) g->vgc_blocks = 1;
+  }
+  return PSC_OK;
+}
+
+static void launch_vgc(psc_graph_s* g, unsigned blocks, const ReachSide& a, const ReachSide& b,
+                       uint32_t tau, uint32_t chunk) {
+  if (vgc_narrow(g))
+    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow><<<blocks, kVgcBlock, 0, g->stream>>>(a, b, tau,
+                                                                                      chunk);
+  else
+    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide><<<blocks, kVgcBlock, 0, g->stream>>>(a, b, tau,
+                                                                                    chunk);
+}
+
 // Largest out-degree (out[0]) and in-degree (out[1]) of the graph.
 __global__ void k_max_degrees(const uint64_t* __restrict__ off, const uint64_t* __restrict__ in_off,
                               uint64_t n, unsigned long long* out) {
@@ -796,11 +830,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
         bool heavy_possible = false;  // some active direction has a vertex above kHeavyDeg
         for (int a = 0; a < na; a++)
           heavy_possible |= g->max_deg[sides[act[a]].backward ? 1 : 0] > kHeavyDeg;
-        if (!g->vgc_blocks) {
-          PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue>, kVgcBlock, 0));
-          if (g->vgc_blocks < 1) g->vgc_blocks = 1;
-        }
+        PSC_TRY(vgc_occupancy(g));
         const unsigned blocks = (unsigned)((uint64_t)g->num_sms * g->vgc_blocks);
         PSC_TRY(zero_counters(g));
         for (int j = 0; j < kVgcChain; j++) {
@@ -818,8 +848,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           }
           {
             ProfScope ps(g, F_REACH_VGC);
-            k_reach_vgc<kVgcBlock, kVgcQueue><<<blocks, kVgcBlock, 0, g->stream>>>(vg[0], vg[1],
-                                                                                 tau, 0u);
+            launch_vgc(g, blocks, vg[0], vg[1], tau, 0u);
           }
           if (heavy_possible) {
             // heavy vertices queued by this round (the kernel returns at once
@@ -906,18 +935,13 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       ProfScope ps(g, F_REACH_VGC);
       // a resident grid; one frontier vertex per warp while the frontier
       // fits it, else chunks of up to 32 so that every warp stays busy
-      if (!g->vgc_blocks) {
-        PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue>, kVgcBlock, 0));
-        if (g->vgc_blocks < 1) g->vgc_blocks = 1;
-      }
+      PSC_TRY(vgc_occupancy(g));
       const uint64_t max_blocks = (uint64_t)g->num_sms * g->vgc_blocks;
       const uint64_t max_warps = max_blocks * (kVgcBlock / 32);
       const uint64_t chunk = std::min<uint64_t>(32, (v_items + max_warps - 1) / max_warps);
       const uint64_t chunks = (v_items + chunk - 1) / chunk;
       const uint64_t blocks = std::min(max_blocks, (chunks + kVgcBlock / 32 - 1) / (kVgcBlock / 32));
-      k_reach_vgc<kVgcBlock, kVgcQueue><<<(unsigned)std::max<uint64_t>(1, blocks), kVgcBlock, 0,
-                                          g->stream>>>(vg[0], vg[1], tau, (uint32_t)chunk);
+      launch_vgc(g, (unsigned)std::max<uint64_t>(1, blocks), vg[0], vg[1], tau, (uint32_t)chunk);
     }
     if (np) {
       ProfScope ps(g, F_REACH_PUSH);

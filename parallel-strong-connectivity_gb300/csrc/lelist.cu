@@ -302,8 +302,10 @@ constexpr uint64_t kLeHeavyMask = (1ull << kLeHeavyShift) - 1;
 // Offers the warp's K candidate pairs key[k] = (p, w[k]) (kEmpty: none):
 // new pairs go to the next frontier and become list entries (w, p, level),
 // and lower next_dist[w]; an insert that gives up after `limit` probes is
-// counted in `fails` (the level is then run again on a larger table).  Called
-// by all 32 lanes.
+// counted in `fails`, and the level is then run again on a larger table.
+// Once a lane of the warp has failed, the warp stops probing and counts its
+// further offers as failures (the rerun makes them all again).  Called by all
+// 32 lanes.
 template <int K>
 __device__ __forceinline__ void le_offer(const uint64_t* __restrict__ off, const uint32_t (&w)[K],
                                          const uint64_t (&key)[K], uint32_t level,
@@ -313,9 +315,12 @@ __device__ __forceinline__ void le_offer(const uint64_t* __restrict__ off, const
                                          uint32_t& fails, unsigned long long& next_edges) {
   const unsigned lane = lane_id();
   uint32_t tm = 0;
+  const bool full = __any_sync(kFull, fails != 0);
 #pragma unroll
   for (int k = 0; k < K; k++)
-    if (key[k] != kEmpty) {
+    if (key[k] != kEmpty && full) {
+      fails++;
+    } else if (key[k] != kEmpty) {
       const int r = table_insert(T, mask, key[k], limit, &probes);
       if (r == 1) {
         tm |= 1u << k;

@@ -78,6 +78,35 @@ def test_lelist_heavy_pairs(sizes, seed):
             assert np.array_equal(dg.lelist(perm, beta), ref)
 
 
+def test_lelist_table_retry():
+    """A batch whose level inserts far more pairs than the previous batch's
+    inserts per edge predict: the pair table overflows its estimate, inserts
+    give up after their probe limit, and the level runs again on a table
+    sized for the worst case.  With beta = 2 the batches are [2^k - 1,
+    2^(k+1) - 1): priority 0 is a hub, priorities 1..254 its leaves (the batch
+    [127, 255) inserts nothing, so the next estimate is the floor), and the
+    batch [255, 511) is a 256-vertex clique that inserts 65,280 pairs at its
+    first level."""
+    leaves, clique, extra = 254, 256, 3000
+    n = 1 + leaves + clique + extra
+    hub = 0
+    lv = np.arange(1, 1 + leaves)
+    cq = np.arange(1 + leaves, 1 + leaves + clique)
+    a, b = np.meshgrid(cq, cq)
+    keep = a != b
+    rng = np.random.default_rng(21)
+    ex = np.arange(1 + leaves + clique, n)
+    # leaves touch only the hub; the clique is its own component
+    src = np.concatenate([np.full(leaves, hub), a[keep], ex, rng.choice(ex, 2000)])
+    dst = np.concatenate([lv, b[keep], rng.choice(ex, len(ex)), rng.choice(ex, 2000)])
+    s = psc.HostGraph.from_edges(n, src, dst).symmetrize()
+    perm = np.concatenate([[hub], lv, cq, rng.permutation(ex)]).astype(np.uint32)
+    ref = O.lelist_seq(s.n, s.off, s.E, perm)
+    with psc.DeviceGraph(s) as dg:
+        assert np.array_equal(dg.lelist(perm, 2.0), ref)
+        assert dg.stats().table_grows >= 1
+
+
 def test_lelist_directed_matches_definition():
     """Distances follow out-edges: the device result equals seq_le_list's
     definition on a directed graph too."""

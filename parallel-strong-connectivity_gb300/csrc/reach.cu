@@ -16,7 +16,7 @@
 //         vertices and scans their in-edges until a frontier bit is found,
 //         then writes the visited / next-frontier words with one store
 //         (the reference's dense_update, no atomics).
-// The push/pull switch follows the reference's rule (judge, reach.hpp:86-112):
+// The push/pull switch follows the reference's rule (REACH::judge, reach.hpp:86-112):
 // push while frontier vertices + their out-edges < m / pull_div (20), with
 // exact degree sums gathered by the kernels instead of sampling.
 //

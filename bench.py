@@ -160,6 +160,10 @@ class Pinned:
         self.ptrs = []
 
 
+# Largest graph the single-thread Tarjan baseline is timed on (a few seconds).
+TARJAN_MAX_EDGES = 2e8
+
+
 def cpu_baseline(g, workload: str, gpu_labels=None, budget_s: float = 15.0,
                  max_runs: int = 20) -> dict:
     """The oracle timed on the host cores; its labels of the first run are
@@ -176,10 +180,20 @@ def cpu_baseline(g, workload: str, gpu_labels=None, budget_s: float = 15.0,
         if runs == 0 and gpu_labels is not None:
             same = bool(np.array_equal(lab, gpu_labels))
         runs += 1
+    # the reference's sequential baseline (baselines/tarjan_scc), one thread,
+    # as an independent check of the partition
+    if g.m <= TARJAN_MAX_EDGES:
+        t = time.perf_counter()
+        tl, k = pyoracle.tarjan(g.n, g.off, g.E)
+        tarjan = {"ms": (time.perf_counter() - t) * 1e3, "threads": 1, "sccs": k,
+                  "partition_equal_gpu": None if gpu_labels is None else
+                  bool(np.array_equal(pyoracle.canon(tl), pyoracle.canon(gpu_labels)))}
+    else:
+        tarjan = {"skipped": f"m > {TARJAN_MAX_EDGES:.0e} edges (bounded CPU sample)"}
     return {"value": g.m * runs / t_total, "unit": "edges/s", "cores": threads, "kind": "port",
             "sample": f"{runs} full SCC solve(s) of the {workload} workload, "
                       f"{t_total / runs * 1e3:.1f} ms each (OpenMP restatement of src/scc.hpp)",
-            "labels_equal_gpu": same}
+            "labels_equal_gpu": same, "tarjan_1thread": tarjan}
 
 
 def dist_setup():

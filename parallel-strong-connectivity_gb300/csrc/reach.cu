@@ -524,6 +524,61 @@ __device__ __forceinline__ bool fb_test(const uint32_t* __restrict__ fb, uint32_
   return (__ldg(&fb[x >> 5]) >> (x & 31)) & 1u;
 }
 
+// Solo scan of one unvisited vertex's in-list [j, lim): kPullP in-edges at a
+// time until a frontier in-neighbour is found.
+__device__ __forceinline__ bool pull_scan(const uint32_t* __restrict__ B_E,
+                                          const uint32_t* __restrict__ fb_in, uint64_t& j,
+                                          uint64_t lim) {
+  bool found = false;
+  while (j < lim && !found) {
+    uint32_t x[kPullP];
+#pragma unroll
+    for (int k = 0; k < kPullP; k++) x[k] = j + k < lim ? __ldg(&B_E[j + k]) : 0xFFFFFFFFu;
+    bool hit[kPullP];
+#pragma unroll
+    for (int k = 0; k < kPullP; k++) hit[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
+    uint64_t step = lim - j < (uint64_t)kPullP ? lim - j : (uint64_t)kPullP;
+#pragma unroll
+    for (int k = kPullP - 1; k >= 0; k--)
+      if (hit[k]) {
+        found = true;
+        step = k + 1;
+      }
+    j += step;
+  }
+  return found;
+}
+
+// The whole warp scans the in-lists left over from the solo phase, one
+// vertex at a time, 32 * kPullP in-edges per step, until a hit.
+__device__ __forceinline__ void pull_long(const uint32_t* __restrict__ B_E,
+                                          const uint32_t* __restrict__ fb_in, uint32_t longm,
+                                          uint64_t j, uint64_t e, bool& found,
+                                          unsigned long long& scanned) {
+  const unsigned lane = lane_id();
+  while (longm) {
+    const int l = __ffs(longm) - 1;
+    longm &= longm - 1;
+    const uint64_t lb = __shfl_sync(kFull, j, l), le = __shfl_sync(kFull, e, l);
+    bool f = false;
+    uint64_t jj = lb;
+    for (; jj < le && !f; jj += 32 * kPullP) {
+      bool hit = false;
+#pragma unroll
+      for (int k = 0; k < kPullP; k++) {
+        const uint64_t q = jj + k * 32 + lane;
+        if (q < le) hit |= fb_test(fb_in, __ldg(&B_E[q]));
+      }
+      f = __any_sync(kFull, hit);
+    }
+    if (lane == 0) scanned += (jj < le ? jj : le) - lb;
+    if (lane == (unsigned)l) found = f;
+  }
+}
+
+// Pull round, two adjacent bitmap words (64 vertices) per warp step: the
+// loads of both words' vertices are issued together, so two dependent chains
+// (visited word, in-list range, first in-edge, frontier bit) overlap.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
     k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
@@ -534,67 +589,58 @@ __global__ void __launch_bounds__(BLOCK)
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint64_t nwords = (n + 31) >> 5;
   unsigned long long cnt = 0, scanned = 0, next_edges = 0, unvisited = 0;
-  for (uint64_t w = gw; w < nwords; w += nw) {
-    const uint64_t v = w * 32 + lane;
-    const uint32_t vw = vis[w];
-    const bool todo = v < n && !((vw >> lane) & 1u);
-    bool found = false;
-    uint64_t j = 0, e = 0;
-    if (todo) {
-      unvisited++;
-      const uint64_t b = B_off[v];
-      e = B_off[v + 1];
-      j = b;
-      const uint64_t lim = e < b + kPullSolo ? e : b + kPullSolo;
-      // the first in-edge alone (dense rounds often hit at once), then
-      // kPullP at a time
-      if (j < lim) {
-        found = fb_test(fb_in, __ldg(&B_E[j]));
-        j++;
-      }
-      while (j < lim && !found) {
-        uint32_t x[kPullP];
-#pragma unroll
-        for (int k = 0; k < kPullP; k++) x[k] = j + k < lim ? __ldg(&B_E[j + k]) : 0xFFFFFFFFu;
-        bool hit[kPullP];
-#pragma unroll
-        for (int k = 0; k < kPullP; k++) hit[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
-        uint64_t step = lim - j < (uint64_t)kPullP ? lim - j : (uint64_t)kPullP;
-#pragma unroll
-        for (int k = kPullP - 1; k >= 0; k--)
-          if (hit[k]) {
-            found = true;
-            step = k + 1;
-          }
-        j += step;
-      }
-      scanned += j - b;
+  for (uint64_t w = gw * 2; w < nwords; w += nw * 2) {
+    const bool two = w + 1 < nwords;
+    const uint64_t v0 = w * 32 + lane, v1 = v0 + 32;
+    const uint32_t vw0 = vis[w], vw1 = two ? vis[w + 1] : ~0u;
+    const bool t0 = v0 < n && !((vw0 >> lane) & 1u);
+    const bool t1 = v1 < n && !((vw1 >> lane) & 1u);
+    uint64_t b0 = 0, e0 = 0, b1 = 0, e1 = 0;
+    if (t0) {
+      b0 = B_off[v0];
+      e0 = B_off[v0 + 1];
     }
-    uint32_t longm = __ballot_sync(kFull, todo && !found && j < e);
-    while (longm) {
-      const int l = __ffs(longm) - 1;
-      longm &= longm - 1;
-      const uint64_t lb = __shfl_sync(kFull, j, l), le = __shfl_sync(kFull, e, l);
-      bool f = false;
-      uint64_t jj = lb;
-      for (; jj < le && !f; jj += 32 * kPullP) {
-        bool hit = false;
-#pragma unroll
-        for (int k = 0; k < kPullP; k++) {
-          const uint64_t q = jj + k * 32 + lane;
-          if (q < le) hit |= fb_test(fb_in, __ldg(&B_E[q]));
-        }
-        f = __any_sync(kFull, hit);
-      }
-      if (lane == 0) scanned += (jj < le ? jj : le) - lb;
-      if (lane == (unsigned)l) found = f;
+    if (t1) {
+      b1 = B_off[v1];
+      e1 = B_off[v1 + 1];
     }
-    if (found) next_edges += A_off[v + 1] - A_off[v];
-    const uint32_t mask = __ballot_sync(kFull, found);
+    unvisited += (t0 ? 1 : 0) + (t1 ? 1 : 0);
+    const uint64_t lim0 = e0 < b0 + kPullSolo ? e0 : b0 + kPullSolo;
+    const uint64_t lim1 = e1 < b1 + kPullSolo ? e1 : b1 + kPullSolo;
+    uint64_t j0 = b0, j1 = b1;
+    // the first in-edge of both vertices together (dense rounds often hit at once)
+    const uint32_t x0 = j0 < lim0 ? __ldg(&B_E[j0]) : 0xFFFFFFFFu;
+    const uint32_t x1 = j1 < lim1 ? __ldg(&B_E[j1]) : 0xFFFFFFFFu;
+    bool f0 = x0 != 0xFFFFFFFFu && fb_test(fb_in, x0);
+    bool f1 = x1 != 0xFFFFFFFFu && fb_test(fb_in, x1);
+    if (j0 < lim0) j0++;
+    if (j1 < lim1) j1++;
+    if (!f0) f0 = pull_scan(B_E, fb_in, j0, lim0);
+    if (!f1) f1 = pull_scan(B_E, fb_in, j1, lim1);
+    if (t0) scanned += j0 - b0;
+    if (t1) scanned += j1 - b1;
+    pull_long(B_E, fb_in, __ballot_sync(kFull, t0 && !f0 && j0 < e0), j0, e0, f0, scanned);
+    pull_long(B_E, fb_in, __ballot_sync(kFull, t1 && !f1 && j1 < e1), j1, e1, f1, scanned);
+    uint64_t o0 = 0, o1 = 0, o0e = 0, o1e = 0;
+    if (f0) {
+      o0 = A_off[v0];
+      o0e = A_off[v0 + 1];
+    }
+    if (f1) {
+      o1 = A_off[v1];
+      o1e = A_off[v1 + 1];
+    }
+    next_edges += (o0e - o0) + (o1e - o1);
+    const uint32_t m0 = __ballot_sync(kFull, f0), m1 = __ballot_sync(kFull, f1);
     if (lane == 0) {
-      fb_out[w] = mask;
-      if (mask) vis[w] = vw | mask;
-      cnt += __popc(mask);
+      fb_out[w] = m0;
+      if (m0) vis[w] = vw0 | m0;
+      cnt += __popc(m0);
+      if (two) {
+        fb_out[w + 1] = m1;
+        if (m1) vis[w + 1] = vw1 | m1;
+        cnt += __popc(m1);
+      }
     }
   }
   scanned = warp_sum(scanned);

@@ -57,7 +57,10 @@ void psc_params_default(psc_params_t* p);
 
 /* Uploads a CSR and its transpose (SCC's constructor, src/scc.hpp:81-92,
  * holds the caller's Graph by reference; this copies it into HBM once).
- * in_off/in_E may be NULL for a symmetric graph (transpose = itself). */
+ * in_off/in_E may be NULL for a symmetric graph (transpose = itself).
+ * All three uploads check the arrays on the device before any other kernel
+ * reads them: offsets from 0 to m, never decreasing, and targets below n;
+ * otherwise PSC_ERR_INVALID (the reference would read out of bounds). */
 int psc_graph_upload(const uint64_t* off, const uint32_t* E, const uint64_t* in_off,
                      const uint32_t* in_E, uint64_t n, uint64_t m, psc_graph_t* out);
 /* Uploads a CSR and builds the transpose on the device
@@ -203,7 +206,10 @@ int psc_server_create(const psc_server_config_t* cfg, psc_server_t* out);
 /* off u64[n+1], E u32[m] (and for SCC optionally the transpose in_off /
  * in_E, as struct Graph carries it; built on the device when NULL) and
  * labels_out stay owned by the caller and must stay valid until
- * psc_server_wait returns for the request's id. */
+ * psc_server_wait returns for the request's id.  Each batch is checked on
+ * the device before it is solved, as the uploads are: a batch holding a
+ * malformed request fails, and psc_server_wait returns PSC_ERR_INVALID for
+ * every request of it. */
 int psc_server_submit(psc_server_t s, int kind, const uint64_t* off, const uint32_t* E,
                       const uint64_t* in_off, const uint32_t* in_E, uint64_t n, uint64_t m,
                       uint64_t seed, void* labels_out, uint64_t* id_out);

@@ -1,5 +1,6 @@
 // Handle lifecycle, scratch buffers, counters, profiling and graph upload
 // for libpsc_cuda.so.  Declared in include/psc.h.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -253,6 +254,36 @@ int alloc_graph_arrays(psc_graph_s* g, bool symmetric) {
 
 // Copies the caller's arrays (host or device) into the handle's graph arrays
 // on its stream and waits for them, so the caller may reuse its buffers.
+// Rejects a CSR whose offsets do not run from 0 to m without decreasing or
+// whose targets are not vertex ids.  Only the arrays themselves are read (no
+// access is indexed by their values), so any input of the declared sizes is
+// safe to check; the traversal kernels, which index by these values, run only
+// on graphs that passed.
+__global__ void k_validate_csr(const uint64_t* __restrict__ off, uint64_t n,
+                               const uint32_t* __restrict__ E, uint64_t m,
+                               unsigned long long* bad) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool b = t == 0 && (off[0] != 0 || off[n] != m);
+  for (uint64_t v = t; v < n; v += stride) b |= off[v] > off[v + 1];
+  for (uint64_t i = t; i < m; i += stride) b |= E[i] >= n;
+  if (__any_sync(kFull, b) && lane_id() == 0) atomicOr(bad, 1ull);
+}
+
+// Checks the graph arrays of a fresh handle (the transpose too when it was
+// given and does not alias); PSC_ERR_INVALID if one is malformed.
+static int validate_graph(psc_graph_s* g, bool with_transpose) {
+  unsigned long long* bad = &g->ctr[2].aux0;  // staging set of the fresh handle
+  PSC_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), g->stream));
+  const unsigned grid = grid_for(g, std::max<uint64_t>(g->n, g->m), 256);
+  k_validate_csr<<<grid, 256, 0, g->stream>>>(g->off, g->n, g->E, g->m, bad);
+  if (with_transpose && g->in_off && g->in_off != g->off)
+    k_validate_csr<<<grid, 256, 0, g->stream>>>(g->in_off, g->n, g->in_E, g->m, bad);
+  PSC_CUDA(cudaGetLastError());
+  PSC_TRY(read_counters(g));
+  return g->hctr[2].aux0 ? PSC_ERR_INVALID : PSC_OK;
+}
+
 static int copy_graph_arrays(psc_graph_s* g, const uint64_t* off, const uint32_t* E,
                              const uint64_t* in_off, const uint32_t* in_E) {
   const uint64_t n = g->n, m = g->m;
@@ -294,6 +325,7 @@ int psc_graph_upload(const uint64_t* off, const uint32_t* E, const uint64_t* in_
   bool sym = in_off == nullptr;
   int s = alloc_graph_arrays(g, sym);
   if (s == PSC_OK) s = copy_graph_arrays(g, off, E, in_off, in_E);
+  if (s == PSC_OK) s = validate_graph(g, true);
   if (s != PSC_OK) {
     psc_graph_free(g);
     return s;
@@ -311,6 +343,7 @@ int psc_graph_upload_device(const uint64_t* d_off, const uint32_t* d_E, const ui
   bool sym = d_in_off == nullptr;
   int s = alloc_graph_arrays(g, sym);
   if (s == PSC_OK) s = copy_graph_arrays(g, d_off, d_E, d_in_off, d_in_E);
+  if (s == PSC_OK) s = validate_graph(g, true);
   if (s != PSC_OK) {
     psc_graph_free(g);
     return s;
@@ -327,6 +360,7 @@ int psc_graph_upload_directed(const uint64_t* off, const uint32_t* E, uint64_t n
   PSC_TRY(make_handle(n, m, &g));
   int s = alloc_graph_arrays(g, false);
   if (s == PSC_OK) s = copy_graph_arrays(g, off, E, nullptr, nullptr);
+  if (s == PSC_OK) s = validate_graph(g, false);  // the transpose build indexes by E
   if (s == PSC_OK) s = build_transpose(g);
   if (s == PSC_OK) {
     cudaError_t e = cudaStreamSynchronize(g->stream);

@@ -84,6 +84,31 @@ __global__ void k_rebase(uint64_t* off, uint64_t n, uint32_t* E, uint64_t m,
   }
 }
 
+// Before the rebase: every request's own offsets run from 0 to its edge count
+// without decreasing and its targets are its vertex ids.  Only the packed
+// arrays are read (no access is indexed by their values); a batch holding a
+// malformed request fails with PSC_ERR_INVALID instead of being traversed.
+__global__ void k_validate_batch(const uint64_t* __restrict__ off, uint64_t n,
+                                 const uint32_t* __restrict__ E, uint64_t m,
+                                 const uint64_t* __restrict__ vbase,
+                                 const uint64_t* __restrict__ ebase, uint32_t R,
+                                 unsigned long long* bad) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool b = false;
+  for (uint64_t i = t; i < n; i += stride) {
+    const uint32_t r = last_le(vbase, R, i);
+    const uint64_t mr = ebase[r + 1] - ebase[r];
+    const uint64_t o = off[i], o2 = i + 1 < vbase[r + 1] ? off[i + 1] : mr;
+    b |= (i == vbase[r] && o != 0) || o > o2 || o2 > mr;
+  }
+  for (uint64_t j = t; j < m; j += stride) {
+    const uint32_t r = last_le(ebase, R, j);
+    b |= E[j] >= vbase[r + 1] - vbase[r];
+  }
+  if (__any_sync(kFull, b) && lane_id() == 0) atomicOr(bad, 1ull);
+}
+
 __global__ void k_put_u64(uint64_t* p, uint64_t v) { *p = v; }
 
 }  // namespace
@@ -158,6 +183,19 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* lau
     std::copy(vbase.begin(), vbase.end(), hb.begin());
     std::copy(ebase.begin(), ebase.end(), hb.begin() + R + 1);
     PSC_CUDA(cudaMemcpyAsync(bases, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    {
+      unsigned long long* bad = &g->ctr[2].aux0;  // staging set of the fresh handle
+      PSC_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), g->stream));
+      const unsigned vgrid = grid_for(g, std::max(n, m), 256);
+      k_validate_batch<<<vgrid, 256, 0, g->stream>>>(g->off, n, g->E, m, bases, bases + R + 1, R,
+                                                      bad);
+      if (with_t)
+        k_validate_batch<<<vgrid, 256, 0, g->stream>>>(g->in_off, n, g->in_E, m, bases,
+                                                        bases + R + 1, R, bad);
+      PSC_CUDA(cudaGetLastError());
+      PSC_TRY(read_counters(g));
+      if (g->hctr[2].aux0) return PSC_ERR_INVALID;
+    }
     k_rebase<<<grid_for(g, n + m, 256), 256, 0, g->stream>>>(g->off, n, g->E, m, bases, bases + R + 1,
                                                               R);
     k_put_u64<<<1, 1, 0, g->stream>>>(g->off + n, m);

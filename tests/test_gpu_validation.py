@@ -1,0 +1,108 @@
+"""Malformed graphs are refused before any traversal kernel reads them: a
+target outside [0, n), offsets that decrease, offsets that do not start at 0
+(device arrays), at upload (host and device arrays, with or without a host
+transpose) and in a server batch.  The checks read only the arrays
+themselves, so these inputs are safe to hand to the device."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import psc
+from psc import _lib
+from psc.server import CC, SCC
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _dev(cuda_device):
+    return cuda_device
+
+
+def good():
+    return psc.HostGraph.rmat(8, 1 << 10, seed=3)
+
+
+def upload(off, E, in_off, in_E, n, m):
+    lib = psc.cuda()
+    h = C.c_void_p()
+    st = lib.psc_graph_upload(off.ctypes.data, E.ctypes.data,
+                              None if in_off is None else in_off.ctypes.data,
+                              None if in_E is None else in_E.ctypes.data, n, m, C.byref(h))
+    if st == 0:
+        lib.psc_graph_free(h)
+    return st
+
+
+def decreasing(off, m):
+    """A copy of off with one interior offset above its successor (ends kept)."""
+    off = off.copy()
+    k = next(i for i in range(1, len(off) - 1) if off[i + 1] < m)
+    off[k] = off[k + 1] + 1
+    return off
+
+
+def test_upload_rejects_a_target_outside_the_graph():
+    g = good()
+    E = g.E.copy()
+    E[len(E) // 2] = g.n
+    assert upload(g.off, E, g.in_off, g.in_E, g.n, g.m) == _lib.PSC_ERR_INVALID
+    in_E = g.in_E.copy()
+    in_E[0] = g.n + 5
+    assert upload(g.off, g.E, g.in_off, in_E, g.n, g.m) == _lib.PSC_ERR_INVALID
+    assert upload(g.off, E, None, None, g.n, g.m) == _lib.PSC_ERR_INVALID
+    assert upload(g.off, g.E, g.in_off, g.in_E, g.n, g.m) == 0
+
+
+def test_upload_rejects_decreasing_offsets():
+    g = good()
+    assert upload(decreasing(g.off, g.m), g.E, g.in_off, g.in_E, g.n, g.m) == _lib.PSC_ERR_INVALID
+    assert upload(g.off, g.E, decreasing(g.in_off, g.m), g.in_E, g.n, g.m) == _lib.PSC_ERR_INVALID
+
+
+def test_directed_upload_checks_before_building_the_transpose():
+    g = good()
+    lib = psc.cuda()
+    E = g.E.copy()
+    E[-1] = 0xFFFFFFFF
+    h = C.c_void_p()
+    assert lib.psc_graph_upload_directed(g.off.ctypes.data, E.ctypes.data, g.n, g.m,
+                                         C.byref(h)) == _lib.PSC_ERR_INVALID
+    assert lib.psc_graph_upload_directed(g.off.ctypes.data, g.E.ctypes.data, g.n, g.m,
+                                         C.byref(h)) == 0
+    lib.psc_graph_free(h)
+
+
+def test_device_upload_checks_the_offset_ends():
+    g = good()
+    lib = psc.cuda()
+    bad = g.off.copy()
+    bad[0] = 1
+    ptrs = []
+    try:
+        for a in (bad, g.E):
+            p = C.c_void_p()
+            assert lib.psc_device_alloc(a.nbytes, C.byref(p)) == 0
+            ptrs.append(p)
+            assert lib.psc_copy(p, a.ctypes.data, a.nbytes) == 0
+        h = C.c_void_p()
+        assert lib.psc_graph_upload_device(ptrs[0], ptrs[1], None, None, g.n, g.m,
+                                           C.byref(h)) == _lib.PSC_ERR_INVALID
+    finally:
+        for p in ptrs:
+            lib.psc_device_free(p)
+
+
+@pytest.mark.parametrize("kind", [SCC, CC])
+def test_server_fails_a_batch_with_a_malformed_request(kind):
+    g = good() if kind == SCC else good().symmetrize()
+    E = g.E.copy()
+    E[3] = g.n  # a vertex id of the next request once packed: still caught
+    bad = psc.HostGraph(g.n, g.m, g.off, E, symmetric=g.symmetric)
+    with psc.Server(workers=1, max_batch=1) as srv:
+        with pytest.raises(psc.PscError) as err:
+            srv.wait(srv.submit(bad, kind, 1))
+        assert err.value.status == _lib.PSC_ERR_INVALID
+        lab, info = srv.wait(srv.submit(g, kind, 1))  # the server keeps serving
+        assert info.status == 0 and len(lab) == g.n

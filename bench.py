@@ -6,10 +6,11 @@ multi-search -> partition -> finalise) of a seeded synthetic graph, the scope
 of the reference's `scc cost` (src/scc.cpp:62-66: graph load and transpose
 excluded).
 
-Default workload: directed 2-D kNN, 10^7 points uniform in the unit square
-(seed 2), k = 5 (m = 5e7), beta 1.5, tau 512, VGC on — the large-diameter
-plain-SCC configuration.  The graph (560 MB with its transpose) is larger than
-the 129 MB L2, so no flush is needed between steps.
+Default workload (the headline line): directed R-MAT, n = 2^26 vertices,
+2^30 draws with (a, b, c, d) = (0.57, 0.19, 0.19, 0.05), seed 3, duplicates
+and self-loops removed (m = 1.06e9), beta 1.5, tau 512, VGC on: the largest
+single-GPU configuration.  The graph (9.6 GB with its transpose) is far larger
+than the 129 MB L2, so no flush is needed between steps.
 
   value   edges/s with the graph resident in HBM (psc_scc_device), timed by
           CUDA events on the library's stream around exactly K steps
@@ -19,11 +20,20 @@ the 129 MB L2, so no flush is needed between steps.
           workload: algorithmic bytes / its event-timed duration vs the
           measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (an OpenMP restatement of the reference's
-          SCC; the reference itself cannot be built) on the same graph
+          SCC, pinned to the reference's own code) on the same graph, with
+          its labels compared to the GPU's
+  connectivity, lelist  the rest of the configuration on the symmetrised
+          graph (m = 2.1e9): GPU time, roofline, the oracle's time and the
+          equality of partition / LE-lists
+  configs  the other configurations measured in the same run (--extras):
+          R-MAT 2^16 (C1), kNN 10^7 x 5 and the 4096^2 grid (C2), the
+          4096-graph batch against per-graph plain solves (C4) and the served
+          stream with p50/p99 per arrival rate against plain solves (C5)
 
-`--impl reference` times that CPU implementation alone as the reference arm.
-Under torchrun (N > 1) each rank runs an independent replica on its own GPU
-(replicas only: a solve does not shard); rank 0 prints the line.
+`--workload` runs one configuration alone (knn, grid, rmat16, rmat22, rmat26,
+batch, serve).  `--impl reference` times the CPU implementation alone as the
+reference arm.  Under torchrun (N > 1) each rank runs an independent replica on
+its own GPU (replicas only: a solve does not shard); rank 0 prints the line.
 """
 from __future__ import annotations
 
@@ -349,7 +359,7 @@ def batch_desc(count: int) -> str:
             "member k seeded 1000+k; packed into one CSR + transpose with a graph-offset table")
 
 
-def run_batch(args, world, rank, local, dist) -> None:
+def run_batch(args, world, rank, local, dist) -> dict | None:
     """Batched SCC: every step solves all graphs of the batch in one lockstep
     call (psc_scc_batch_device); compared with per-graph plain solves of a
     stratified sample of the same graphs on the same GPU."""
@@ -476,13 +486,13 @@ def run_batch(args, world, rank, local, dist) -> None:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_batch(g, vb, seeds, sample)
+        cpu = cpu_baseline_batch(g, vb, seeds, sample, budget_s=args.cpu_budget)
 
     lib.psc_device_free(d_labels.value)
     dg.free()
     pin.free()
     if rank != 0:
-        return
+        return None
     line = {
         "metric": "batched SCC graphs/s", "value": value, "unit": "graphs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -514,7 +524,7 @@ def run_batch(args, world, rank, local, dist) -> None:
         "clocks": clocks,
         "gpu_launches": launches,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 SERVE = dict(pool=48, seed0=5000, log10_min=3.0, log10_max=7.0, cc_share=0.2,
@@ -549,7 +559,7 @@ def _unit(seed: int) -> float:
     return (x >> 11) / float(1 << 53)
 
 
-def run_serve(args, world, rank, local, dist) -> None:
+def run_serve(args, world, rank, local, dist) -> dict | None:
     """Served stream: Poisson arrivals of SCC (80 %) and connectivity (20 %)
     requests drawn from a seeded pool, through the request server
     (continuous batching, 120 GiB admission budget); latency p50/p99 and
@@ -687,7 +697,7 @@ def run_serve(args, world, rank, local, dist) -> None:
     plain_rate = nreq / plain_s
     pin.free()
     if rank != 0:
-        return
+        return None
     top = sweep[-1]
     line = {
         "metric": "served SCC/CC graphs/s", "value": sat["graphs_per_s"], "unit": "graphs/s",
@@ -715,7 +725,7 @@ def run_serve(args, world, rank, local, dist) -> None:
         "roofline": None, "cpu_baseline": None, "clocks": clocks,
         "gpu_launches": sat["launches"],
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
@@ -759,7 +769,7 @@ def roofline_of(prof: dict, steps: int, workload: str = "") -> dict:
     }
 
 
-def run_gpu(args, world, rank, local, dist) -> None:
+def run_gpu(args, world, rank, local, dist) -> dict | None:
     import psc
     from psc import _lib
 
@@ -846,7 +856,7 @@ def run_gpu(args, world, rank, local, dist) -> None:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(g, args.workload, ref_labels)
+        cpu = cpu_baseline(g, args.workload, ref_labels, budget_s=args.cpu_budget)
         if cpu["labels_equal_gpu"] is False:
             raise SystemExit("GPU labels differ from the oracle's")
 
@@ -855,7 +865,7 @@ def run_gpu(args, world, rank, local, dist) -> None:
     pin.free()
     extra = cc_le_extra(psc, g, rank, world, args) if args.workload == "rmat26" else {}
     if rank != 0:
-        return
+        return None
     line = {
         "metric": "SCC edges/s", "value": value, "unit": "edges/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -879,35 +889,94 @@ def run_gpu(args, world, rank, local, dist) -> None:
         "gpu_launches": launches,
     }
     line.update(extra)
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def cc_le_extra(psc, g, rank, world, args) -> dict:
     """The rest of the R-MAT 2^26 configuration: connectivity and LE-lists
     (permutation seed 4) on the symmetrised graph, resident on the device,
-    with the oracle's connectivity timed beside it (rank 0)."""
+    each with the roofline of its dominant kernel family, and (rank 0, one
+    replica) the oracle's connectivity and parallel LE-lists on the host
+    cores: their time as the CPU baseline and their output as the check."""
     t = time.perf_counter()
     s = g.symmetrize()
     log(f"[rank {rank}] symmetrised: m = {s.m} in {time.perf_counter() - t:.1f}s")
     out = {}
+    perm = psc.random_permutation(s.n, 4)
     with psc.DeviceGraph(s) as dg:
         lab = dg.cc()
         cc_ms = min((dg.cc(), dg.stats().total_ms)[1] for _ in range(3))
-        perm = psc.random_permutation(s.n, 4)
+        dg.set_profiling(True)
+        dg.profile_reset()
+        dg.cc()
+        cc_roof = roofline_of(dg.profile(), 1)
+        dg.set_profiling(False)
         le = dg.lelist(perm)
         le_ms = min((dg.lelist(perm), dg.stats().total_ms)[1] for _ in range(2))
+        dg.set_profiling(True)
+        dg.profile_reset()
+        dg.lelist(perm)
+        le_roof = roofline_of(dg.profile(), 1)
+        dg.set_profiling(False)
     out["connectivity"] = {"ms": cc_ms, "edges_per_s": s.m / (cc_ms / 1e3), "m_sym": s.m,
-                           "components": int(len(np.unique(lab)))}
-    out["lelist"] = {"ms": le_ms, "triples": int(len(le)), "perm_seed": 4}
+                           "components": int(len(np.unique(lab))), "roofline": cc_roof}
+    out["lelist"] = {"ms": le_ms, "triples": int(len(le)), "perm_seed": 4, "roofline": le_roof}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
         import pyoracle
+        threads = os.cpu_count() or 1
         t = time.perf_counter()
-        ref = pyoracle.cc(s.n, s.off, s.E, nthreads=os.cpu_count() or 1)
+        ref = pyoracle.cc(s.n, s.off, s.E, nthreads=threads)
         cpu_ms = (time.perf_counter() - t) * 1e3
-        out["connectivity"]["cpu_ms"] = cpu_ms
+        out["connectivity"]["cpu_baseline"] = {
+            "ms": cpu_ms, "cores": threads, "kind": "port",
+            "sample": "one connectivity solve (OpenMP restatement of src/Connectivity.h)"}
         out["connectivity"]["partition_equal_oracle"] = bool(
             np.array_equal(pyoracle.canon(ref), pyoracle.canon(lab)))
+        del ref
+        if not args.no_le_check:
+            t = time.perf_counter()
+            ref_le = pyoracle.lelist_par(s.n, s.off, s.E, perm, nthreads=threads)
+            cpu_ms = (time.perf_counter() - t) * 1e3
+            out["lelist"]["cpu_baseline"] = {
+                "ms": cpu_ms, "cores": threads, "kind": "port",
+                "sample": "one LE-list solve (OpenMP restatement of src/LeList.hpp:219-328)"}
+            out["lelist"]["equal_oracle"] = bool(ref_le.shape == le.shape and
+                                                 np.array_equal(ref_le, le))
+            if not out["lelist"]["equal_oracle"]:
+                raise SystemExit("GPU LE-lists differ from the oracle's")
+        if not out["connectivity"]["partition_equal_oracle"]:
+            raise SystemExit("GPU connectivity partition differs from the oracle's")
+    return out
+
+
+# Keys of a workload's line kept when it rides on the headline line.
+EXTRA_KEYS = ("metric", "value", "unit", "ms_per_step", "speedup_vs_plain", "plain", "e2e",
+              "roofline", "cpu_baseline", "latency_ms", "sweep", "saturated", "clocks",
+              "gpu_launches")
+
+
+def run_extras(args, world, rank, local, dist) -> dict:
+    """The other configurations, each measured as its own workload would be
+    (fewer CPU-baseline seconds) and summarised under the headline line."""
+    out = {}
+    for name in [x for x in args.extras.split(",") if x and x != "none"]:
+        sub = argparse.Namespace(**vars(args))
+        sub.workload = name
+        sub.cpu_budget = min(args.cpu_budget, 5.0)
+        t = time.perf_counter()
+        if name == "batch":
+            line = run_batch(sub, world, rank, local, dist)
+        elif name == "serve":
+            line = run_serve(sub, world, rank, local, dist)
+        else:
+            line = run_gpu(sub, world, rank, local, dist)
+        log(f"[rank {rank}] extra {name}: {time.perf_counter() - t:.1f}s")
+        if line is not None:
+            cfg = line.get("config", {})
+            key = cfg.get("workload", name)
+            out[key] = {k: line[k] for k in EXTRA_KEYS if k in line}
+            out[key]["config"] = {k: v for k, v in cfg.items() if k not in ("phase_ms",)}
     return out
 
 
@@ -917,7 +986,16 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["psc", "reference"], default="psc")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "serve"], default="knn")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "serve"], default="rmat26",
+                    help="headline workload (default: R-MAT 2^26, the largest single-GPU "
+                         "configuration, with its connectivity and LE-lists)")
+    ap.add_argument("--extras", default="rmat16,knn,grid,batch,serve",
+                    help="with the rmat26 headline: other configurations measured in the same "
+                         "run and summarised under its line ('none' for the headline alone)")
+    ap.add_argument("--cpu-budget", type=float, default=15.0,
+                    help="seconds of CPU-baseline solves on the host cores")
+    ap.add_argument("--no-le-check", action="store_true",
+                    help="rmat26: skip the oracle's LE-lists (check and CPU baseline)")
     ap.add_argument("--serve-requests", type=int, default=SERVE["requests"],
                     help="requests per arrival rate of the serve workload")
     ap.add_argument("--serve-workers", type=int, default=4)
@@ -943,12 +1021,19 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, world, rank, dist)
-        elif args.workload == "batch":
-            run_batch(args, world, rank, local, dist)
+            return
+        if args.workload == "batch":
+            line = run_batch(args, world, rank, local, dist)
         elif args.workload == "serve":
-            run_serve(args, world, rank, local, dist)
+            line = run_serve(args, world, rank, local, dist)
         else:
-            run_gpu(args, world, rank, local, dist)
+            line = run_gpu(args, world, rank, local, dist)
+        if args.workload == "rmat26":
+            extras = run_extras(args, world, rank, local, dist)
+            if line is not None:
+                line["configs"] = extras
+        if line is not None:
+            print(json.dumps(line), flush=True)
     finally:
         if dist is not None:
             dist.destroy_process_group()

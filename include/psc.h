@@ -76,6 +76,17 @@ uint64_t psc_graph_num_vertices(psc_graph_t g);
 uint64_t psc_graph_num_edges(psc_graph_t g);
 /* Copies the device transpose back (in_off u64[n+1], in_E u32[m]). */
 int psc_graph_download_transpose(psc_graph_t g, uint64_t* in_off, uint32_t* in_E);
+/* Uploads a directed CSR (host or device memory) and symmetrises it on the
+ * device: make_symmetric (src/graph.hpp:187-220) -- every edge in both
+ * directions, each adjacency list sorted, duplicate edges and self-loops
+ * dropped -- as read_graph(.., symmetric = true) does (:248-277).  The handle
+ * holds the symmetric graph: psc_graph_num_edges gives its edge count,
+ * psc_graph_download its arrays.  The input is checked as psc_graph_upload
+ * checks it (PSC_ERR_INVALID). */
+int psc_graph_upload_symmetrize(const uint64_t* off, const uint32_t* E, uint64_t n, uint64_t m,
+                                psc_graph_t* out);
+/* Copies the handle's CSR back (off u64[n+1], E u32[m]). */
+int psc_graph_download(psc_graph_t g, uint64_t* off, uint32_t* E);
 
 /* SCC::scc (src/scc.hpp:277-476).  labels_out: host u64[n], the reference's
  * sequence<size_t> (final value = (label & 0xFFFFFFFF) - 1). */
@@ -206,10 +217,13 @@ int psc_server_create(const psc_server_config_t* cfg, psc_server_t* out);
 /* off u64[n+1], E u32[m] (and for SCC optionally the transpose in_off /
  * in_E, as struct Graph carries it; built on the device when NULL) and
  * labels_out stay owned by the caller and must stay valid until
- * psc_server_wait returns for the request's id.  Each batch is checked on
- * the device before it is solved, as the uploads are: a batch holding a
- * malformed request fails, and psc_server_wait returns PSC_ERR_INVALID for
- * every request of it. */
+ * psc_server_wait returns for the request's id; off and in_off are host
+ * memory.  Checks: at submission, off[0] = 0 and off[n] = m (in_off the
+ * same); on the device, before its batch is solved, every offset of the
+ * request no larger than the next and every target below n (the checks of
+ * psc_graph_upload).  A malformed request fails alone: psc_server_wait
+ * returns PSC_ERR_INVALID for it, and the other requests of its batch are
+ * solved without it. */
 int psc_server_submit(psc_server_t s, int kind, const uint64_t* off, const uint32_t* E,
                       const uint64_t* in_off, const uint32_t* in_E, uint64_t n, uint64_t m,
                       uint64_t seed, void* labels_out, uint64_t* id_out);
@@ -238,7 +252,9 @@ int psc_server_destroy(psc_server_t s);
  * file-scope __device__ array sized for PSC_NOALLOC_MAX_VERTICES vertices,
  * about 34 MB, which every GPU that loads the library holds until the
  * process exits.  Larger graphs are rejected with PSC_ERR_TOO_LARGE before
- * any device work.
+ * any device work.  The arrays are checked on the device before any kernel
+ * indexes by them, as psc_graph_upload checks its input (offsets from 0 to m,
+ * never decreasing; targets below n): PSC_ERR_INVALID otherwise.
  *
  * The first call on a device looks up that array's device address
  * (cudaGetSymbolAddress) with the device current; make that first call before

@@ -7,15 +7,14 @@
  * CPU-baseline / reference arm may load this library, and only as the checker
  * or the timed CPU baseline; the product library never calls it.
  *
- * Parity status: the reference cannot be compiled (its ParlayLib submodule is
- * empty and it has no test vectors).  The oracle is pinned at the partition
- * level against scipy.sparse.csgraph (strong and weak components) and an
- * iterative restatement of the reference's own Tarjan baseline, and at the
- * LE-list level against the reference's sequential definition
- * (src/LeList.hpp:76-115), via the fixtures in tests/golden/.  Raw SCC label
- * values are a deterministic function of (graph, pivot permutation); the
- * permutation is this project's documented Feistel bijection because
- * parlay::random_shuffle is unavailable.
+ * Parity status: pinned to the reference's own code.  The reference's headers
+ * compile unmodified against this project's ParlayLib-API stand-in
+ * (oracle/ref_shim/, oracle/ref.mk -> oracle/_ref/), whose hashes and
+ * permutations are the ones used here; tests/golden/ref_vectors.npz holds
+ * what that build computes (raw SCC labels, reach sets, transpose,
+ * symmetrisation, connectivity partitions, BFS distances, LE-lists) and
+ * tests/test_ref_pin.py holds this oracle to it bit for bit.  Partition-level
+ * fixtures from scipy (tests/golden/graphs.npz) stay as an independent check.
  *
  * Graph layout everywhere: CSR offsets u64[n+1], targets u32[m] and the
  * transpose (in_off, in_E), as struct Graph in src/graph.hpp:35-43.

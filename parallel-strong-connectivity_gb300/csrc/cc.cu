@@ -731,6 +731,14 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
     }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(read_counters(g));
+    if (g->profiling) {
+      // algorithmic bytes: push / VGC: 16 per frontier vertex (range), 8 per
+      // edge (target id, label CAS), 8 per new vertex; pull: both bitmaps,
+      // 8 per scanned in-edge, 4 per new vertex
+      const Counters& c = g->hctr[0];
+      g->prof[F_CC].bytes += pull ? 0.25 * n + 8.0 * c.edges + 4.0 * c.next
+                                  : 16.0 * nf + 8.0 * c.edges + 8.0 * c.next;
+    }
     nf = g->hctr[0].next;
     nf_edges = g->hctr[0].next_edges;
   }
@@ -815,6 +823,14 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
   // from one side: an edge skipped on both sides joins two vertices already
   // in the largest component.
   constexpr uint32_t kUfSample = 2;
+  // algorithmic bytes of a union pass: per vertex its range, its two labels
+  // and its cluster; per offered edge the target id and its label
+  auto uf_bytes = [&](unsigned long long edges0) -> int {
+    if (!g->profiling) return PSC_OK;
+    PSC_TRY(read_counters(g));
+    g->prof[F_UF].bytes += 28.0 * n + 8.0 * (g->hctr[0].edges - edges0) + 8.0 * n;
+    return PSC_OK;
+  };
   {
     ProfScope ps(g, F_UF);
     k_uf_edges<kCcBlock><<<grid_for(g, n, tb), tb, 0, g->stream>>>(
@@ -824,6 +840,8 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
     ProfScope ps(g, F_UF);
     k_uf_final<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, n);
   }
+  PSC_TRY(uf_bytes(0));
+  const unsigned long long uf_edges1 = g->profiling ? g->hctr[0].edges : 0;
   uint32_t max_root = 0;
   if (batched) {
     ProfScope ps(g, F_UF);
@@ -844,6 +862,7 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
     ProfScope ps(g, F_UF);
     k_uf_final<<<grid_for(g, n, tb), tb, 0, g->stream>>>(d_label, n);
   }
+  PSC_TRY(uf_bytes(uf_edges1));
   PSC_CUDA(cudaGetLastError());
   if (n_forest) {
     PSC_TRY(read_counters(g));

@@ -251,6 +251,23 @@ inline unsigned grid_for(psc_graph_s* g, uint64_t items, unsigned block, unsigne
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
+// Rejects a CSR whose offsets do not run from 0 to m without decreasing or
+// whose targets are not vertex ids: sets *bad.  Only the arrays themselves
+// are read (no access is indexed by their values), so any input of the
+// declared sizes is safe to check.  A template so that every translation
+// unit that launches it holds its own instance.
+template <int kUnused = 0>
+__global__ void k_validate_csr(const uint64_t* __restrict__ off, uint64_t n,
+                               const uint32_t* __restrict__ E, uint64_t m,
+                               unsigned long long* bad) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool b = t == 0 && (off[0] != 0 || off[n] != m);
+  for (uint64_t v = t; v < n; v += stride) b |= off[v] > off[v + 1];
+  for (uint64_t i = t; i < m; i += stride) b |= E[i] >= n;
+  if (__any_sync(kFull, b) && lane_id() == 0) atomicOr(bad, 1ull);
+}
+
 __device__ __forceinline__ uint64_t ld_cg(const uint64_t* p) { return __ldcg((const unsigned long long*)p); }
 __device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) { return __ldcg(p); }
 

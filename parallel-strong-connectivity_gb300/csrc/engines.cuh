@@ -20,6 +20,10 @@ int call_end(psc_graph_s* g);
 
 // Builds in_off/in_E from off/E on the device (in-lists sorted by source).
 int build_transpose(psc_graph_s* g);
+// Replaces off/E by their symmetrisation on the device (both directions,
+// lists sorted, duplicates and self-loops dropped; g->m becomes the new edge
+// count) and makes g symmetric.
+int build_symmetric(psc_graph_s* g);
 
 // Single-source reachability into the bitmap vis (u32[ceil(n/32)], cleared
 // here).  backward = expand over the transpose.  rounds receives the number

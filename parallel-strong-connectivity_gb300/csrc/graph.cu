@@ -254,31 +254,17 @@ int alloc_graph_arrays(psc_graph_s* g, bool symmetric) {
 
 // Copies the caller's arrays (host or device) into the handle's graph arrays
 // on its stream and waits for them, so the caller may reuse its buffers.
-// Rejects a CSR whose offsets do not run from 0 to m without decreasing or
-// whose targets are not vertex ids.  Only the arrays themselves are read (no
-// access is indexed by their values), so any input of the declared sizes is
-// safe to check; the traversal kernels, which index by these values, run only
-// on graphs that passed.
-__global__ void k_validate_csr(const uint64_t* __restrict__ off, uint64_t n,
-                               const uint32_t* __restrict__ E, uint64_t m,
-                               unsigned long long* bad) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  bool b = t == 0 && (off[0] != 0 || off[n] != m);
-  for (uint64_t v = t; v < n; v += stride) b |= off[v] > off[v + 1];
-  for (uint64_t i = t; i < m; i += stride) b |= E[i] >= n;
-  if (__any_sync(kFull, b) && lane_id() == 0) atomicOr(bad, 1ull);
-}
-
+// Malformed arrays are refused by k_validate_csr (common.cuh) before any
+// traversal kernel, which indexes by their values, runs on them.
 // Checks the graph arrays of a fresh handle (the transpose too when it was
 // given and does not alias); PSC_ERR_INVALID if one is malformed.
 static int validate_graph(psc_graph_s* g, bool with_transpose) {
   unsigned long long* bad = &g->ctr[2].aux0;  // staging set of the fresh handle
   PSC_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), g->stream));
   const unsigned grid = grid_for(g, std::max<uint64_t>(g->n, g->m), 256);
-  k_validate_csr<<<grid, 256, 0, g->stream>>>(g->off, g->n, g->E, g->m, bad);
+  k_validate_csr<><<<grid, 256, 0, g->stream>>>(g->off, g->n, g->E, g->m, bad);
   if (with_transpose && g->in_off && g->in_off != g->off)
-    k_validate_csr<<<grid, 256, 0, g->stream>>>(g->in_off, g->n, g->in_E, g->m, bad);
+    k_validate_csr<><<<grid, 256, 0, g->stream>>>(g->in_off, g->n, g->in_E, g->m, bad);
   PSC_CUDA(cudaGetLastError());
   PSC_TRY(read_counters(g));
   return g->hctr[2].aux0 ? PSC_ERR_INVALID : PSC_OK;
@@ -371,6 +357,37 @@ int psc_graph_upload_directed(const uint64_t* off, const uint32_t* E, uint64_t n
     return s;
   }
   *out = g;
+  return PSC_OK;
+}
+
+int psc_graph_upload_symmetrize(const uint64_t* off, const uint32_t* E, uint64_t n, uint64_t m,
+                                psc_graph_t* out) {
+  if (!out || !off || (m && !E) || n == 0 || n >= 0xFFFFFFFFull || m >= (1ull << 39))
+    return PSC_ERR_INVALID;
+  psc_graph_s* g = nullptr;
+  PSC_TRY(make_handle(n, m, &g));
+  int s = alloc_graph_arrays(g, true);
+  if (s == PSC_OK) s = copy_graph_arrays(g, off, E, nullptr, nullptr);
+  if (s == PSC_OK) s = validate_graph(g, false);  // the pair build indexes by off and E
+  if (s == PSC_OK) s = build_symmetric(g);
+  if (s == PSC_OK) {
+    cudaError_t e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) s = cuda_status(e);
+  }
+  if (s != PSC_OK) {
+    psc_graph_free(g);
+    return s;
+  }
+  *out = g;
+  return PSC_OK;
+}
+
+int psc_graph_download(psc_graph_t g, uint64_t* off, uint32_t* E) {
+  if (!g || !off || (g->m && !E)) return PSC_ERR_INVALID;
+  PSC_CUDA(cudaSetDevice(g->device));
+  PSC_CUDA(cudaStreamSynchronize(g->stream));
+  PSC_CUDA(cudaMemcpy(off, g->off, (g->n + 1) * 8, cudaMemcpyDeviceToHost));
+  if (g->m) PSC_CUDA(cudaMemcpy(E, g->E, g->m * 4, cudaMemcpyDeviceToHost));
   return PSC_OK;
 }
 

@@ -242,6 +242,14 @@ int bfs_run(psc_graph_s* g, uint32_t src, uint32_t* dist, uint32_t* rounds_out) 
     }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(read_counters(g));
+    if (g->profiling) {
+      // push: 16 per frontier vertex, 8 per edge (id, distance), 8 per new
+      // vertex; pull: both bitmaps, 16 per unvisited vertex, 8 per scanned
+      // in-edge, 4 per new vertex
+      const Counters& c = g->hctr[0];
+      g->prof[F_LE].bytes += pull ? 0.25 * n + 16.0 * c.unvisited + 8.0 * c.edges + 4.0 * c.next
+                                  : 16.0 * nf + 8.0 * c.edges + 8.0 * c.next;
+    }
     nf = g->hctr[0].next;
     nf_edges = g->hctr[0].next_edges;
   }
@@ -920,6 +928,10 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
                      (unsigned long long)cap, attempts, ms);
       }
       const uint64_t added = g->hctr[0].next;
+      if (g->profiling)  // 8 per pair + 16 per range, 8 per edge (id,
+                         // distance), 8 per probe, 16 per new pair (list entry)
+        g->prof[F_LE].bytes += 24.0 * nf + 8.0 * g->hctr[0].edges + 8.0 * g->hctr[0].probes +
+                               16.0 * added;
       ratio_next.push_back((double)added / (double)std::max<uint64_t>(bound, 1));
       ne += added;
       L += added;
@@ -948,6 +960,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   PSC_CUDA(cudaMemsetAsync(cnt, 0, (n + 1) * 4, g->stream));
   {
     ProfScope ps(g, F_LE_SORT);
+    ps.bytes = 8.0 * L;
     k_le_count<<<grid_for(g, L, tb), tb, 0, g->stream>>>(Lk, L, cnt);
   }
   PSC_TRY(scan_emit(g, n, CountValue{cnt}, BucketOffsets{boff, cursor}, nullptr, F_LE_SORT));
@@ -955,6 +968,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   PSC_CUDA(cudaMemcpyAsync(boff + n, &g->hctr[3].aux1, 8, cudaMemcpyHostToDevice, g->stream));
   {
     ProfScope ps(g, F_LE_SORT);
+    ps.bytes = 20.0 * L;
     k_le_scatter<<<grid_for(g, L, tb), tb, 0, g->stream>>>(Lk, Ld, L, boff, cursor, Bk);
   }
   uint32_t* big;
@@ -962,6 +976,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   PSC_TRY(zero_counters(g));
   {
     ProfScope ps(g, F_LE_SORT);
+    ps.bytes = 8.0 * n + 16.0 * L;
     k_seg_sort_small<<<grid_for(g, n, tb), tb, 0, g->stream>>>(boff, n, Bk, big, g->ctr);
   }
   PSC_TRY(read_counters(g));
@@ -977,6 +992,7 @@ int lelist_run(psc_graph_s* g, const uint32_t* centers, double beta, uint64_t* l
   }
   {
     ProfScope ps(g, F_LE_SORT);
+    ps.bytes = 16.0 * n + 9.0 * L;  // bucket bounds, the filter's pass and keep flags
     if (nbig)
       k_seg_sort_u64<<<sgrid, kSegBlock, 0, g->stream>>>(big, nbig, boff, Bk, scratch, slen);
     k_le_filter<<<grid_for(g, n, tb), tb, 0, g->stream>>>(boff, n, Bk, keep);

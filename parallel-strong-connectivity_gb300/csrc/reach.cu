@@ -17,8 +17,11 @@
 //         then writes the visited / next-frontier words with one store
 //         (the reference's dense_update, no atomics).
 // The push/pull switch follows the reference's rule (REACH::judge, reach.hpp:86-112):
-// push while frontier vertices + their out-edges < m / pull_div (20), with
-// exact degree sums gathered by the kernels instead of sampling.
+// push while frontier vertices + their out-edges < m / pull_div (20).  After a
+// push round the out-edge count is exact (gathered by the kernels); after a
+// pull round it is exact for a frontier under 2^14 vertices and otherwise
+// estimated from 50 sampled frontier vertices, as the reference's
+// dense_sample does (reach.hpp:192-206).
 //
 // Expansion issues K edges per lane before using any of them, so the loads of
 // E and the claims on the bitmap overlap instead of forming one dependent
@@ -519,6 +522,10 @@ __global__ void __launch_bounds__(BLOCK) k_reach_heavy(ReachSide s0, ReachSide s
 // a time, 32 * kPullP edges per step, until a hit.
 constexpr int kPullP = 4;
 constexpr uint32_t kPullSolo = 64;
+#ifndef PSC_PULL_W
+#define PSC_PULL_W 4
+#endif
+constexpr int kPullW = PSC_PULL_W;  // bitmap words per warp step
 
 __device__ __forceinline__ bool fb_test(const uint32_t* __restrict__ fb, uint32_t x) {
   return (__ldg(&fb[x >> 5]) >> (x & 31)) & 1u;
@@ -576,82 +583,146 @@ __device__ __forceinline__ void pull_long(const uint32_t* __restrict__ B_E,
   }
 }
 
-// Pull round, two adjacent bitmap words (64 vertices) per warp step: the
-// loads of both words' vertices are issued together, so two dependent chains
-// (visited word, in-list range, first in-edge, frontier bit) overlap.
-template <int BLOCK>
+// Pull round, W adjacent bitmap words (32 W vertices) per warp step: the
+// loads of all W words' vertices are issued together, so W dependent chains
+// (visited word, in-list range, first in-edge, frontier bit) overlap.  The
+// next round's out-edge count is left to k_pull_out_edges, off this chain.
+template <int BLOCK, int W>
 __global__ void __launch_bounds__(BLOCK)
     k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
-                 const uint64_t* __restrict__ A_off, const uint32_t* __restrict__ fb_in,
-                 uint32_t* vis, uint32_t* fb_out, uint64_t n, Counters* ctr) {
+                 const uint32_t* __restrict__ fb_in, uint32_t* vis, uint32_t* fb_out, uint64_t n,
+                 Counters* ctr) {
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
   const uint64_t nwords = (n + 31) >> 5;
-  unsigned long long cnt = 0, scanned = 0, next_edges = 0, unvisited = 0;
-  for (uint64_t w = gw * 2; w < nwords; w += nw * 2) {
-    const bool two = w + 1 < nwords;
-    const uint64_t v0 = w * 32 + lane, v1 = v0 + 32;
-    const uint32_t vw0 = vis[w], vw1 = two ? vis[w + 1] : ~0u;
-    const bool t0 = v0 < n && !((vw0 >> lane) & 1u);
-    const bool t1 = v1 < n && !((vw1 >> lane) & 1u);
-    uint64_t b0 = 0, e0 = 0, b1 = 0, e1 = 0;
-    if (t0) {
-      b0 = B_off[v0];
-      e0 = B_off[v0 + 1];
+  unsigned long long cnt = 0, scanned = 0, unvisited = 0;
+  for (uint64_t w = gw * W; w < nwords; w += nw * W) {
+    uint32_t vw[W];
+    bool t[W], f[W];
+    uint64_t b[W], e[W], j[W], lim[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) vw[k] = w + k < nwords ? vis[w + k] : ~0u;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+      const uint64_t v = (w + k) * 32 + lane;
+      t[k] = v < n && !((vw[k] >> lane) & 1u);
+      b[k] = e[k] = 0;
+      if (t[k]) {
+        b[k] = B_off[v];
+        e[k] = B_off[v + 1];
+      }
+      unvisited += t[k] ? 1 : 0;
     }
-    if (t1) {
-      b1 = B_off[v1];
-      e1 = B_off[v1 + 1];
+    // the first in-edge of all W vertices together (dense rounds often hit
+    // at once)
+    uint32_t x[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+      lim[k] = e[k] < b[k] + kPullSolo ? e[k] : b[k] + kPullSolo;
+      j[k] = b[k];
+      x[k] = j[k] < lim[k] ? __ldg(&B_E[j[k]]) : 0xFFFFFFFFu;
     }
-    unvisited += (t0 ? 1 : 0) + (t1 ? 1 : 0);
-    const uint64_t lim0 = e0 < b0 + kPullSolo ? e0 : b0 + kPullSolo;
-    const uint64_t lim1 = e1 < b1 + kPullSolo ? e1 : b1 + kPullSolo;
-    uint64_t j0 = b0, j1 = b1;
-    // the first in-edge of both vertices together (dense rounds often hit at once)
-    const uint32_t x0 = j0 < lim0 ? __ldg(&B_E[j0]) : 0xFFFFFFFFu;
-    const uint32_t x1 = j1 < lim1 ? __ldg(&B_E[j1]) : 0xFFFFFFFFu;
-    bool f0 = x0 != 0xFFFFFFFFu && fb_test(fb_in, x0);
-    bool f1 = x1 != 0xFFFFFFFFu && fb_test(fb_in, x1);
-    if (j0 < lim0) j0++;
-    if (j1 < lim1) j1++;
-    if (!f0) f0 = pull_scan(B_E, fb_in, j0, lim0);
-    if (!f1) f1 = pull_scan(B_E, fb_in, j1, lim1);
-    if (t0) scanned += j0 - b0;
-    if (t1) scanned += j1 - b1;
-    pull_long(B_E, fb_in, __ballot_sync(kFull, t0 && !f0 && j0 < e0), j0, e0, f0, scanned);
-    pull_long(B_E, fb_in, __ballot_sync(kFull, t1 && !f1 && j1 < e1), j1, e1, f1, scanned);
-    uint64_t o0 = 0, o1 = 0, o0e = 0, o1e = 0;
-    if (f0) {
-      o0 = A_off[v0];
-      o0e = A_off[v0 + 1];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+      f[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
+      if (j[k] < lim[k]) j[k]++;
     }
-    if (f1) {
-      o1 = A_off[v1];
-      o1e = A_off[v1 + 1];
-    }
-    next_edges += (o0e - o0) + (o1e - o1);
-    const uint32_t m0 = __ballot_sync(kFull, f0), m1 = __ballot_sync(kFull, f1);
-    if (lane == 0) {
-      fb_out[w] = m0;
-      if (m0) vis[w] = vw0 | m0;
-      cnt += __popc(m0);
-      if (two) {
-        fb_out[w + 1] = m1;
-        if (m1) vis[w + 1] = vw1 | m1;
-        cnt += __popc(m1);
+#pragma unroll
+    for (int k = 0; k < W; k++)
+      if (!f[k]) f[k] = pull_scan(B_E, fb_in, j[k], lim[k]);
+#pragma unroll
+    for (int k = 0; k < W; k++)
+      if (t[k]) scanned += j[k] - b[k];
+#pragma unroll
+    for (int k = 0; k < W; k++)
+      pull_long(B_E, fb_in, __ballot_sync(kFull, t[k] && !f[k] && j[k] < e[k]), j[k], e[k], f[k],
+                scanned);
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+      const uint32_t mk = __ballot_sync(kFull, f[k]);
+      if (lane == 0 && w + k < nwords) {
+        fb_out[w + k] = mk;
+        if (mk) vis[w + k] = vw[k] | mk;
+        cnt += __popc(mk);
       }
     }
   }
   scanned = warp_sum(scanned);
-  next_edges = warp_sum(next_edges);
   unvisited = warp_sum(unvisited);
   if (lane == 0) {
     if (cnt) atomicAdd(&ctr->next, cnt);
     if (scanned) atomicAdd(&ctr->edges, scanned);
-    if (next_edges) atomicAdd(&ctr->next_edges, next_edges);
     if (unvisited) atomicAdd(&ctr->unvisited, unvisited);
   }
+}
+
+// Out-edges of the frontier a pull round left in fb (ctr->next vertices),
+// for the next round's push / pull choice (REACH::judge, src/reach.hpp:86-112).
+// A small frontier (under kPullExactBelow) gets its exact degree sum over the
+// whole grid, as the reference packs it and sums its degrees; a larger one an
+// estimate from the degrees of 50 frontier vertices met by hashed probes
+// hash32(seed + i) % n, i = 1, 2, ..., times the frontier size
+// (REACH::dense_sample, :192-206), done by the first warp of the grid (at
+// most kSampleProbes probes; no hit gives 0).  Writes ctr->next_edges.
+// A pull round's grid: the resident blocks of the kernel (a grid-stride loop
+// covers the rest), fewer when the bitmap has fewer warp steps than that.
+template <int BLOCK>
+static unsigned pull_grid(int num_sms, uint64_t nwords) {
+  static int per_sm = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_reach_pull<BLOCK, kPullW>, BLOCK, 0) !=
+            cudaSuccess ||
+        b < 1) {
+      cudaGetLastError();
+      b = 1;
+    }
+    return b;
+  }();
+  const uint64_t steps = (nwords + kPullW - 1) / kPullW;
+  const uint64_t want = (steps + BLOCK / 32 - 1) / (BLOCK / 32);
+  const uint64_t cap = (uint64_t)num_sms * per_sm;
+  return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+constexpr uint64_t kPullExactBelow = 1u << 14;
+constexpr uint32_t kSampleProbes = 32 * 64;
+constexpr uint32_t kSampleHits = 50;
+
+__global__ void k_pull_out_edges(const uint32_t* __restrict__ fb, const uint64_t* __restrict__ A_off,
+                                 uint64_t n, uint32_t seed, Counters* ctr) {
+  const unsigned lane = lane_id();
+  const uint64_t nf = *(volatile unsigned long long*)&ctr->next;
+  if (nf < kPullExactBelow) {
+    const uint64_t nwords = (n + 31) >> 5;
+    unsigned long long sum = 0;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nwords;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+      uint32_t word = fb[w];
+      while (word) {
+        const uint64_t v = w * 32 + (__ffs(word) - 1);
+        word &= word - 1;
+        sum += A_off[v + 1] - A_off[v];
+      }
+    }
+    sum = warp_sum(sum);
+    if (lane == 0 && sum) atomicAdd(&ctr->next_edges, sum);
+    return;
+  }
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  unsigned long long sum = 0;
+  uint32_t hits = 0;
+  for (uint32_t base = 1; base <= kSampleProbes && hits < kSampleHits; base += 32) {
+    const uint32_t idx = (uint32_t)(hash32(seed + base + lane) % n);
+    const bool hit = fb_test(fb, idx);
+    const uint32_t m = __ballot_sync(kFull, hit);
+    const uint32_t rank = __popc(m & ((1u << lane) - 1));
+    if (hit && hits + rank < kSampleHits) sum += A_off[idx + 1] - A_off[idx];
+    hits += __popc(m);
+  }
+  sum = warp_sum(sum);
+  if (hits > kSampleHits) hits = kSampleHits;
+  if (lane == 0) ctr->next_edges = hits ? nf * (sum / hits) : 0;
 }
 
 __global__ void k_queue_to_bitmap(const uint32_t* __restrict__ q, uint64_t nq, uint32_t* fb) {
@@ -1014,18 +1085,20 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       uint32_t* fbo = (uint32_t*)g->bufs[s.slot_fb].p;
       switch (g->block) {
         case 128:
-          k_reach_pull<128><<<grid_for(g, nwords * 32, 128), 128, 0, g->stream>>>(
-              B_off, B_E, A_off, fa, s.vis, fbo, n, g->ctr + s.cset);
+          k_reach_pull<128, kPullW><<<pull_grid<128>(g->num_sms, nwords), 128, 0, g->stream>>>(
+              B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
           break;
         case 512:
-          k_reach_pull<512><<<grid_for(g, nwords * 32, 512), 512, 0, g->stream>>>(
-              B_off, B_E, A_off, fa, s.vis, fbo, n, g->ctr + s.cset);
+          k_reach_pull<512, kPullW><<<pull_grid<512>(g->num_sms, nwords), 512, 0, g->stream>>>(
+              B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
           break;
         default:
-          k_reach_pull<kReachBlock><<<grid_for(g, nwords * 32, kReachBlock), kReachBlock, 0,
-                                      g->stream>>>(B_off, B_E, A_off, fa, s.vis, fbo, n,
-                                                   g->ctr + s.cset);
+          k_reach_pull<kReachBlock, kPullW>
+              <<<pull_grid<kReachBlock>(g->num_sms, nwords), kReachBlock, 0, g->stream>>>(
+                  B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
       }
+      k_pull_out_edges<<<grid_for(g, nwords, 256), 256, 0, g->stream>>>(
+          fbo, A_off, n, hash32((uint32_t)s.rounds), g->ctr + s.cset);
     }
     PSC_CUDA(cudaGetLastError());
     cudaEvent_t tr_b = nullptr;
@@ -1235,6 +1308,17 @@ extern "C" int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E,
   Counters* ctr = (Counters*)(nd.scratch + kNaCtr);
   Counters hc;  // host copy of the counters (stack memory)
 
+  // the caller's arrays are checked before any kernel indexes by them (the
+  // check of psc_graph_upload; the flag is a word of the counters region)
+  PSC_CUDA(cudaMemsetAsync(ctr, 0, sizeof(Counters), s));
+  const unsigned vgrid = na_grid(nd.num_sms, std::max<uint64_t>(n, m), 256);
+  k_validate_csr<><<<vgrid, 256, 0, s>>>(d_off, n, d_E, m, &ctr->aux0);
+  if (d_in_off != d_off)
+    k_validate_csr<><<<vgrid, 256, 0, s>>>(d_in_off, n, d_in_E, m, &ctr->aux0);
+  PSC_CUDA(cudaGetLastError());
+  PSC_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  PSC_CUDA(cudaStreamSynchronize(s));
+  if (hc.aux0) return PSC_ERR_INVALID;
   // the array keeps the previous call's contents: clear the visited bitmap
   PSC_CUDA(cudaMemsetAsync(vis, 0, nwords * 4, s));
   k_reach_init<<<1, 1, 0, s>>>(vis, qa, src);
@@ -1261,11 +1345,25 @@ extern "C" int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E,
       ReachSide none{};
       k_reach_push<kReachBlock><<<na_grid(nd.num_sms, nf, kReachBlock), kReachBlock, 0, s>>>(side,
                                                                                           none);
-      k_reach_heavy<kReachBlock><<<nd.num_sms * 4, kReachBlock, 0, s>>>(side, none);
+      PSC_CUDA(cudaGetLastError());
+      PSC_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+      PSC_CUDA(cudaStreamSynchronize(s));
+      // vertices above the heavy threshold were listed: the whole grid
+      // expands them before the round ends
+      if (hc.heavy)
+        k_reach_heavy<kReachBlock><<<nd.num_sms * 4, kReachBlock, 0, s>>>(side, none);
       std::swap(qa, qb);
+      if (!hc.heavy) {
+        nf = hc.next;
+        nf_edges = hc.next_edges;
+        continue;
+      }
     } else {
-      k_reach_pull<kReachBlock><<<na_grid(nd.num_sms, nwords * 32, kReachBlock), kReachBlock, 0, s>>>(
-          B_off, B_E, A_off, fa, vis, fb, n, ctr);
+      k_reach_pull<kReachBlock, kPullW>
+          <<<pull_grid<kReachBlock>(nd.num_sms, nwords), kReachBlock, 0, s>>>(
+              B_off, B_E, fa, vis, fb, n, ctr);
+      k_pull_out_edges<<<na_grid(nd.num_sms, nwords, 256), 256, 0, s>>>(fb, A_off, n,
+                                                                        hash32(r), ctr);
       std::swap(fa, fb);
     }
     PSC_CUDA(cudaGetLastError());

@@ -86,13 +86,14 @@ __global__ void k_rebase(uint64_t* off, uint64_t n, uint32_t* E, uint64_t m,
 
 // Before the rebase: every request's own offsets run from 0 to its edge count
 // without decreasing and its targets are its vertex ids.  Only the packed
-// arrays are read (no access is indexed by their values); a batch holding a
-// malformed request fails with PSC_ERR_INVALID instead of being traversed.
+// arrays are read (no access is indexed by their values).  A malformed item
+// sets its request's flag (bad[r]) and the any-flag (*any), so that only the
+// requests that hold one fail and the rest of the batch runs without them.
 __global__ void k_validate_batch(const uint64_t* __restrict__ off, uint64_t n,
                                  const uint32_t* __restrict__ E, uint64_t m,
                                  const uint64_t* __restrict__ vbase,
                                  const uint64_t* __restrict__ ebase, uint32_t R,
-                                 unsigned long long* bad) {
+                                 unsigned long long* bad, unsigned long long* any) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool b = false;
@@ -100,13 +101,19 @@ __global__ void k_validate_batch(const uint64_t* __restrict__ off, uint64_t n,
     const uint32_t r = last_le(vbase, R, i);
     const uint64_t mr = ebase[r + 1] - ebase[r];
     const uint64_t o = off[i], o2 = i + 1 < vbase[r + 1] ? off[i + 1] : mr;
-    b |= (i == vbase[r] && o != 0) || o > o2 || o2 > mr;
+    if ((i == vbase[r] && o != 0) || o > o2 || o2 > mr) {
+      atomicOr(&bad[r], 1ull);
+      b = true;
+    }
   }
   for (uint64_t j = t; j < m; j += stride) {
     const uint32_t r = last_le(ebase, R, j);
-    b |= E[j] >= vbase[r + 1] - vbase[r];
+    if (E[j] >= vbase[r + 1] - vbase[r]) {
+      atomicOr(&bad[r], 1ull);
+      b = true;
+    }
   }
-  if (__any_sync(kFull, b) && lane_id() == 0) atomicOr(bad, 1ull);
+  if (__any_sync(kFull, b) && lane_id() == 0) atomicOr(any, 1ull);
 }
 
 __global__ void k_put_u64(uint64_t* p, uint64_t v) { *p = v; }
@@ -136,8 +143,12 @@ namespace {
 
 constexpr uint64_t kUrgentEdges = 1ull << 26;
 
-// Solves one batch of requests of the same kind on a fresh handle.
-int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* launches) {
+// Solves one batch of requests of the same kind on a fresh handle.  When the
+// device check finds malformed requests, returns PSC_ERR_INVALID with
+// bad[k] = 1 for each of them (and nothing solved); the caller runs the rest
+// again without them.
+int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* launches,
+              std::vector<char>* bad_out) {
   const uint32_t R = (uint32_t)B.size();
   std::vector<uint64_t> vbase(R + 1, 0), ebase(R + 1, 0);
   for (uint32_t k = 0; k < R; k++) {
@@ -177,24 +188,33 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* lau
                                    g->stream));
       }
     }
+    // bases: vbase[R+1], ebase[R+1], then one malformed-flag word per request
     uint64_t* bases;
-    PSC_TRY(ensure_t(g, B_SCHED, 2 * (size_t)R + 2, &bases));
-    std::vector<uint64_t> hb(2 * (size_t)R + 2);
+    PSC_TRY(ensure_t(g, B_SCHED, 3 * (size_t)R + 2, &bases));
+    std::vector<uint64_t> hb(3 * (size_t)R + 2, 0);
     std::copy(vbase.begin(), vbase.end(), hb.begin());
     std::copy(ebase.begin(), ebase.end(), hb.begin() + R + 1);
     PSC_CUDA(cudaMemcpyAsync(bases, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, g->stream));
     {
-      unsigned long long* bad = &g->ctr[2].aux0;  // staging set of the fresh handle
-      PSC_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), g->stream));
+      unsigned long long* any = &g->ctr[2].aux0;  // staging set of the fresh handle
+      unsigned long long* flags = (unsigned long long*)(bases + 2 * (size_t)R + 2);
+      PSC_CUDA(cudaMemsetAsync(any, 0, sizeof(unsigned long long), g->stream));
       const unsigned vgrid = grid_for(g, std::max(n, m), 256);
       k_validate_batch<<<vgrid, 256, 0, g->stream>>>(g->off, n, g->E, m, bases, bases + R + 1, R,
-                                                      bad);
+                                                      flags, any);
       if (with_t)
         k_validate_batch<<<vgrid, 256, 0, g->stream>>>(g->in_off, n, g->in_E, m, bases,
-                                                        bases + R + 1, R, bad);
+                                                        bases + R + 1, R, flags, any);
       PSC_CUDA(cudaGetLastError());
       PSC_TRY(read_counters(g));
-      if (g->hctr[2].aux0) return PSC_ERR_INVALID;
+      if (g->hctr[2].aux0) {
+        std::vector<uint64_t> hf(R);
+        PSC_CUDA(cudaMemcpyAsync(hf.data(), flags, R * 8, cudaMemcpyDeviceToHost, g->stream));
+        PSC_CUDA(cudaStreamSynchronize(g->stream));
+        bad_out->assign(R, 0);
+        for (uint32_t k = 0; k < R; k++) (*bad_out)[k] = hf[k] != 0;
+        return PSC_ERR_INVALID;
+      }
     }
     k_rebase<<<grid_for(g, n + m, 256), 256, 0, g->stream>>>(g->off, n, g->E, m, bases, bases + R + 1,
                                                               R);
@@ -291,7 +311,29 @@ void worker_loop(psc_server_s* S) {
       r->batch_size = (uint32_t)batch.size();
     }
     uint64_t launches = 0;
-    const int st = run_batch(S, batch, kind, &launches);
+    // malformed requests fail alone: the rest of the batch runs again
+    // without them (at most once per malformed request)
+    std::vector<Request*> run = batch, failed;
+    int st = PSC_OK;
+    while (!run.empty()) {
+      std::vector<char> bad;
+      uint64_t l = 0;
+      st = run_batch(S, run, kind, &l, &bad);
+      launches += l;
+      if (st != PSC_ERR_INVALID || bad.empty()) break;
+      std::vector<Request*> keep;
+      for (size_t k = 0; k < run.size(); k++) {
+        if (bad[k]) {
+          run[k]->status = PSC_ERR_INVALID;
+          failed.push_back(run[k]);
+        } else {
+          keep.push_back(run[k]);
+        }
+      }
+      if (keep.size() == run.size()) break;  // flags without a flagged request
+      run.swap(keep);
+      st = PSC_OK;
+    }
     const auto t1 = Clock::now();
     {
       std::lock_guard<std::mutex> lk(S->mu);
@@ -299,12 +341,15 @@ void worker_loop(psc_server_s* S) {
       S->used -= bytes;
       S->running--;
       S->stats.busy_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+      for (auto* r : run) {
+        r->status = st;
+        r->batch_size = (uint32_t)run.size();
+      }
       for (auto* r : batch) {
         r->t_done = t1;
-        r->status = st;
         r->done = true;
         S->stats.completed++;
-        if (st != PSC_OK) S->stats.failed++;
+        if (r->status != PSC_OK) S->stats.failed++;
       }
     }
     S->done_cv.notify_all();

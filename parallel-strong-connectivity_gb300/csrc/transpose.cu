@@ -279,4 +279,169 @@ int build_transpose(psc_graph_s* g) {
   return PSC_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Device symmetrisation (make_symmetric, src/graph.hpp:187-220): every edge in
+// both directions, each adjacency list sorted, duplicates and self-loops
+// dropped.  The 2m pairs (a, b) -- a's list holds b -- are sorted by b and
+// then stably by a with the radix passes above (an LSD sort of the key
+// (a, b)); one compaction keeps the first pair of every run of equal pairs
+// when a != b, writing the targets; out-degrees come from the run lengths of
+// the kept sources.
+// ---------------------------------------------------------------------------
+__global__ void k_sym_pairs(const uint32_t* __restrict__ E, const uint32_t* __restrict__ src,
+                            uint64_t m, uint32_t* key, uint32_t* val) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = src[i], b = E[i];
+    key[i] = b;  // first pass set: sort by the target
+    val[i] = a;
+    key[m + i] = a;  // the reverse edge b -> a
+    val[m + i] = b;
+  }
+}
+
+struct SymKeep {  // first of a run of equal (a, b) pairs, a != b
+  const uint32_t* A;
+  const uint32_t* B;
+  __device__ uint32_t operator()(uint64_t i) const {
+    const uint32_t a = A[i], b = B[i];
+    if (a == b) return 0u;
+    return (i == 0 || A[i - 1] != a || B[i - 1] != b) ? 1u : 0u;
+  }
+};
+
+struct SymEmit {
+  const uint32_t* A;
+  const uint32_t* B;
+  uint32_t* a_out;
+  uint32_t* b_out;
+  __device__ void operator()(uint64_t i, uint64_t excl, uint32_t v) const {
+    if (v) {
+      a_out[excl] = A[i];
+      b_out[excl] = B[i];
+    }
+  }
+};
+
+// Stable LSD radix sort of cnt (key, val) pairs by the low `bits` bits of
+// key, from (k[0], v[0]) through (k[1], v[1]) and back; *at receives the
+// index of the pair of buffers holding the result.
+static int radix_pairs(psc_graph_s* g, uint64_t cnt, int bits, uint32_t* k[2], uint32_t* v[2],
+                       uint32_t* hist, uint64_t* offs, int* at) {
+  const int passes = (bits + kRsBits - 1) / kRsBits;
+  const uint64_t ntiles = (cnt + kRsTile - 1) / kRsTile;
+  const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)g->num_sms * 8);
+  int cur = 0;
+  for (int p = 0; p < passes; p++) {
+    const int shift = p * kRsBits;
+    {
+      ProfScope ps(g, F_TRANSPOSE);
+      ps.bytes = 4.0 * cnt;
+      k_rs_hist<<<grid, kRsBlock, 0, g->stream>>>(k[cur], cnt, shift, ntiles, hist);
+    }
+    PSC_TRY(scan_emit(g, (uint64_t)kRsBins * ntiles, HistValue{hist}, HistEmit{offs}, nullptr,
+                      F_TRANSPOSE));
+    {
+      ProfScope ps(g, F_TRANSPOSE);
+      ps.bytes = 16.0 * cnt;
+      k_rs_scatter<<<grid, kRsBlock, 0, g->stream>>>(k[cur], v[cur], cnt, shift, ntiles, offs,
+                                                     k[cur ^ 1], v[cur ^ 1]);
+    }
+    cur ^= 1;
+  }
+  *at = cur;
+  return PSC_OK;
+}
+
+static void release(psc_graph_s* g, int b) {
+  DevBuf& d = g->bufs[b];
+  if (d.p) cudaFreeAsync(d.p, g->stream);
+  d.p = nullptr;
+  d.bytes = 0;
+}
+
+int build_symmetric(psc_graph_s* g) {
+  const uint64_t n = g->n, m = g->m;
+  uint64_t* off_s = nullptr;
+  uint32_t* E_s = nullptr;
+  uint64_t ms = 0;
+  uint32_t* cnt;
+  PSC_TRY(ensure_t(g, B_TMP32, n + 1, &cnt));
+  PSC_CUDA(cudaMemsetAsync(cnt, 0, (n + 1) * 4, g->stream));
+  if (m > 0) {
+    const uint64_t c = 2 * m;
+    int bits = 1;
+    while (bits < 32 && ((uint64_t)1 << bits) < n) bits++;
+    const uint64_t ntiles = (c + kRsTile - 1) / kRsTile;
+    uint32_t *k[2], *v[2], *hist, *asel;
+    uint64_t* offs;
+    PSC_TRY(ensure_t(g, B_AUX0, c, &k[0]));
+    PSC_TRY(ensure_t(g, B_AUX1, c, &v[0]));
+    PSC_TRY(ensure_t(g, B_AUX2, c, &k[1]));
+    PSC_TRY(ensure_t(g, B_QA, c, &v[1]));
+    PSC_TRY(ensure_t(g, B_AUX3, (uint64_t)kRsBins * ntiles, &hist));
+    PSC_TRY(ensure_t(g, B_SCAN2, (uint64_t)kRsBins * ntiles + 1, &offs));
+    {
+      ProfScope ps(g, F_TRANSPOSE);
+      ps.bytes = 16.0 * n + 4.0 * m;
+      k_edge_sources<<<grid_for(g, (m + kSrcRun - 1) / kSrcRun * 32, 256), 256, 0, g->stream>>>(
+          g->off, n, m, v[1]);
+    }
+    {
+      ProfScope ps(g, F_TRANSPOSE);
+      ps.bytes = 8.0 * m + 16.0 * m;
+      k_sym_pairs<<<grid_for(g, m, 256), 256, 0, g->stream>>>(g->E, v[1], m, k[0], v[0]);
+    }
+    int at = 0;
+    PSC_TRY(radix_pairs(g, c, bits, k, v, hist, offs, &at));  // by target
+    // second pass set: the sources become the keys
+    uint32_t* k2[2] = {v[at], k[at ^ 1]};
+    uint32_t* v2[2] = {k[at], v[at ^ 1]};
+    PSC_TRY(radix_pairs(g, c, bits, k2, v2, hist, offs, &at));  // stably by source
+    const uint32_t* A = k2[at];
+    const uint32_t* B = v2[at];
+    release(g, B_AUX3);
+    release(g, B_SCAN2);
+    // the kept pairs: targets and sources into the free pair of buffers
+    asel = v2[at ^ 1];
+    uint32_t* bsel = k2[at ^ 1];
+    PSC_TRY(scan_emit_flags(g, c, SymKeep{A, B}, SymEmit{A, B, asel, bsel}, &ms, F_TRANSPOSE,
+                            8.0, 8.0));
+    PSC_CUDA(cudaMallocAsync((void**)&E_s, (ms ? ms : 1) * 4, g->stream));
+    if (ms) PSC_CUDA(cudaMemcpyAsync(E_s, bsel, ms * 4, cudaMemcpyDeviceToDevice, g->stream));
+    if (ms) {
+      uint64_t* rs;
+      PSC_TRY(ensure_t(g, B_SCAN3, n + 1, &rs));
+      ProfScope ps(g, F_TRANSPOSE);
+      ps.bytes = 8.0 * ms;
+      k_run_starts<<<grid_for(g, ms, 256), 256, 0, g->stream>>>(asel, ms, rs);
+      k_run_lengths<<<grid_for(g, ms, 256), 256, 0, g->stream>>>(asel, ms, rs, cnt);
+    }
+    release(g, B_AUX0);
+    release(g, B_AUX1);
+    release(g, B_AUX2);
+    release(g, B_QA);
+    release(g, B_SCAN3);
+  } else {
+    PSC_CUDA(cudaMallocAsync((void**)&E_s, 4, g->stream));
+  }
+  PSC_CUDA(cudaMallocAsync((void**)&off_s, (n + 1) * 8, g->stream));
+  uint64_t total = 0;
+  PSC_TRY(scan_emit(g, n, CntValue{cnt}, OffEmit{off_s, cnt}, &total, F_TRANSPOSE));
+  PSC_CUDA(cudaMemcpyAsync(off_s + n, &ms, 8, cudaMemcpyHostToDevice, g->stream));
+  PSC_CUDA(cudaStreamSynchronize(g->stream));  // ms lives on this stack frame
+  release(g, B_TMP32);
+  if (g->in_off && g->in_off != g->off) cudaFreeAsync(g->in_off, g->stream);
+  if (g->in_E && g->in_E != g->E) cudaFreeAsync(g->in_E, g->stream);
+  cudaFreeAsync(g->off, g->stream);
+  cudaFreeAsync(g->E, g->stream);
+  g->off = g->in_off = off_s;
+  g->E = g->in_E = E_s;
+  g->m = ms;
+  g->symmetric = true;
+  PSC_CUDA(cudaGetLastError());
+  return PSC_OK;
+}
+
 }  // namespace psc

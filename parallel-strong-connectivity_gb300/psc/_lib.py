@@ -109,6 +109,8 @@ CUDA_SIGNATURES = {
     "psc_graph_num_vertices": (U64, [P]),
     "psc_graph_num_edges": (U64, [P]),
     "psc_graph_download_transpose": (I32, [P, P, P]),
+    "psc_graph_upload_symmetrize": (I32, [P, P, U64, U64, C.POINTER(P)]),
+    "psc_graph_download": (I32, [P, P, P]),
     "psc_scc": (I32, [P, C.POINTER(Params), P]),
     "psc_scc_device": (I32, [P, C.POINTER(Params), P]),
     "psc_reach": (I32, [P, U32, I32, I32, U32, P, C.POINTER(U32)]),

@@ -253,6 +253,26 @@ class DeviceGraph:
               "psc_graph_upload_directed")
         return DeviceGraph(handle=h.value)
 
+    @staticmethod
+    def symmetrized(off: np.ndarray, E: np.ndarray) -> "DeviceGraph":
+        """Upload a directed CSR and symmetrise it on the device
+        (make_symmetric semantics, src/graph.hpp:187-220)."""
+        lib = _lib.cuda()
+        off = np.ascontiguousarray(off, dtype=np.uint64)
+        E = np.ascontiguousarray(E, dtype=np.uint32)
+        h = C.c_void_p()
+        check(lib.psc_graph_upload_symmetrize(_ptr(off), _ptr(E) if len(E) else None,
+                                              len(off) - 1, len(E), C.byref(h)),
+              "psc_graph_upload_symmetrize")
+        return DeviceGraph(handle=h.value)
+
+    def download(self) -> tuple[np.ndarray, np.ndarray]:
+        """The handle's CSR (off u64[n+1], E u32[m]) in host memory."""
+        off = np.empty(self.n + 1, np.uint64)
+        E = np.empty(max(self.m, 1), np.uint32)
+        check(self._lib.psc_graph_download(self.h, _ptr(off), _ptr(E)), "psc_graph_download")
+        return off, E[: self.m]
+
     def free(self) -> None:
         if getattr(self, "h", None):
             self._lib.psc_graph_free(self.h)

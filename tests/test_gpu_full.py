@@ -49,3 +49,13 @@ def test_cc_knn_full(knn):
     with psc.DeviceGraph(s) as dg:
         lab = dg.cc()
     assert np.array_equal(O.canon(lab), O.canon(O.cc(s.n, s.off, s.E)))
+
+
+def test_device_symmetrize_knn_full(knn):
+    """make_symmetric on the device (two radix sorts of 10^8 pairs) equals
+    the host library's, bit for bit."""
+    s = knn.symmetrize()
+    with psc.DeviceGraph.symmetrized(knn.off, knn.E) as dg:
+        assert dg.m == s.m
+        off, E = dg.download()
+    assert np.array_equal(off, s.off) and np.array_equal(E, s.E)

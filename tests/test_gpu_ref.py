@@ -54,3 +54,13 @@ def test_cc_bfs_lelist_equal_reference(name):
         ref_check(c, "bfs", dg.bfs(0))
         if g.n >= 2:
             ref_check(c, "le", dg.lelist(psc.random_permutation(s.n, REF_LE_SEED)))
+
+
+@pytest.mark.parametrize("name", ref_names())
+def test_device_symmetrize_equals_reference(name):
+    c, g = ref_vectors()[name], ref_graph(name)
+    with psc.DeviceGraph.symmetrized(g.off, g.E) as dg:
+        so, sE = dg.download()
+        ref_check(c, "sym_off", so)
+        ref_check(c, "sym_E", sE)
+        ref_check(c, "cc", canon(dg.cc()))

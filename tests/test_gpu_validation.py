@@ -106,3 +106,55 @@ def test_server_fails_a_batch_with_a_malformed_request(kind):
         assert err.value.status == _lib.PSC_ERR_INVALID
         lab, info = srv.wait(srv.submit(g, kind, 1))  # the server keeps serving
         assert info.status == 0 and len(lab) == g.n
+
+
+@pytest.mark.parametrize("kind", [SCC, CC])
+def test_server_malformed_request_fails_alone_in_its_batch(kind):
+    """A malformed request packed beside good ones fails alone: the others
+    are solved (the batch runs again without it) and equal their solo
+    solves."""
+    def sym(g):
+        return g if kind == SCC else g.symmetrize()
+
+    goods = [sym(psc.HostGraph.rmat(8, 1 << 10, seed=s)) for s in (3, 4)]
+    b = sym(psc.HostGraph.rmat(8, 1 << 10, seed=5))
+    E = b.E.copy()
+    E[7] = b.n + 2
+    bad = psc.HostGraph(b.n, b.m, b.off, E, symmetric=b.symmetric)
+    blocker = sym(psc.HostGraph.knn(1_000_000, 5, seed=9))
+    with psc.Server(workers=1, max_batch=8) as srv:
+        # the worker is busy with the blocker while the next three queue up,
+        # so they are taken as one batch
+        r0 = srv.submit(blocker, kind, 1)
+        ids = [srv.submit(goods[0], kind, 11), srv.submit(bad, kind, 12),
+               srv.submit(goods[1], kind, 13)]
+        srv.wait(r0)
+        outs = []
+        for rid in (ids[0], ids[2]):
+            lab, info = srv.wait(rid)
+            assert info.status == 0
+            outs.append((lab, info))
+        with pytest.raises(psc.PscError) as err:
+            srv.wait(ids[1])
+        assert err.value.status == _lib.PSC_ERR_INVALID
+    assert max(info.batch_size for _, info in outs) >= 2, "the requests were not batched"
+    for g, (lab, _), seed in zip(goods, outs, (11, 13)):
+        with psc.DeviceGraph(g) as dg:
+            if kind == SCC:
+                assert np.array_equal(lab, dg.scc(psc.default_params(seed=seed)))
+            else:
+                import pyoracle as O
+                assert np.array_equal(O.canon(lab), O.canon(dg.cc()))
+
+
+def test_symmetrize_upload_rejects_a_malformed_graph():
+    g = good()
+    E = g.E.copy()
+    E[-1] = g.n
+    lib = psc.cuda()
+    h = C.c_void_p()
+    assert lib.psc_graph_upload_symmetrize(g.off.ctypes.data, E.ctypes.data, g.n, g.m,
+                                           C.byref(h)) == _lib.PSC_ERR_INVALID
+    off = decreasing(g.off, g.m)
+    assert lib.psc_graph_upload_symmetrize(off.ctypes.data, g.E.ctypes.data, g.n, g.m,
+                                           C.byref(h)) == _lib.PSC_ERR_INVALID

@@ -7,7 +7,11 @@ The test plays such a caller: it owns the graph and output buffers, passes
 them in, and checks that two calls in a row give exactly what the allocating
 entry point psc_reach gives (exact equality: the output is a 0/1 flag per
 vertex).  It also checks that graphs above the fixed scratch limit are
-refused before any device work.  This file is collected last so that a
+refused before any device work, that a graph of exactly the limit (which
+fills the fixed bitmaps, queues and heavy list) gives the same sets, that a
+malformed graph is refused, and that a call takes no device memory (the
+device's free memory is the same before and after it).  This file is
+collected last so that a
 failure here cannot hide the other tests; it passes alone in a fresh process
 as well as after them.
 """
@@ -119,3 +123,66 @@ def test_noalloc_rejects_graphs_above_the_limit():
         assert b"psc_reach_noalloc" in lib.psc_strerror(st)
     finally:
         small.free()
+
+
+def test_noalloc_at_the_vertex_limit():
+    """n = 2^21 exactly (R-MAT, 16 draws per vertex): from the hub the search
+    expands a vertex of the heavy list, switches to pull rounds and back to
+    push rounds; from a second source the previous call's state must not
+    leak."""
+    g = psc.HostGraph.rmat(21, 16 << 21, seed=25)
+    assert g.n == 1 << 21
+    arrays = DeviceArrays(g)
+    try:
+        with psc.DeviceGraph(g) as dg:
+            for src in (0, 12345):
+                for backward in (False, True):
+                    got = arrays.reach(src, backward)
+                    assert np.array_equal(got, dg.reach(src, backward=backward))
+        ref = O.reach_seq(g.n, g.off, g.E, 0)
+        got = arrays.reach(0, False)
+        assert np.array_equal(got, ref)
+        assert got.sum() > g.n // 4
+    finally:
+        arrays.free()
+
+
+def test_noalloc_refuses_a_malformed_graph():
+    g = psc.HostGraph.rmat(10, 1 << 13, seed=26)
+    E = g.E.copy()
+    E[len(E) // 3] = g.n + 1
+    bad = psc.HostGraph(g.n, g.m, g.off, E, g.in_off, g.in_E)
+    arrays = DeviceArrays(bad)
+    try:
+        r = C.c_uint32()
+        st = arrays.lib.psc_reach_noalloc(arrays.off, arrays.E, arrays.in_off, arrays.in_E, g.n,
+                                          g.m, 0, 0, arrays.dst, None, C.byref(r))
+        assert st == _lib.PSC_ERR_INVALID
+    finally:
+        arrays.free()
+    good = DeviceArrays(g)  # the next call on a good graph is unaffected
+    try:
+        assert np.array_equal(good.reach(0, False), O.reach_seq(g.n, g.off, g.E, 0))
+    finally:
+        good.free()
+
+
+def test_noalloc_takes_no_device_memory():
+    """Free device memory (cudaMemGetInfo, through torch) is unchanged across
+    calls, once a first pass of the same calls has loaded the kernels they
+    use (lazy module loading takes device memory for code)."""
+    torch = pytest.importorskip("torch")
+    g = psc.HostGraph.rmat(16, 1 << 20, seed=27)
+    arrays = DeviceArrays(g)
+    calls = [(0, False), (0, True), (99, True), (4321, False)]
+    try:
+        for src, backward in calls:
+            arrays.reach(src, backward)
+        torch.cuda.synchronize()
+        before = torch.cuda.mem_get_info(0)[0]
+        for src, backward in calls:
+            arrays.reach(src, backward)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info(0)[0] == before
+    finally:
+        arrays.free()

@@ -132,6 +132,13 @@ int psc_cc(psc_graph_t g, double beta, uint32_t* labels_out, uint32_t* forest_ou
  * (optional) host u32[n] = BFS-tree parent inside the cluster (parent[v] = v
  * for centres), the reference's spanning_tree output. */
 int psc_ldd(psc_graph_t g, double beta, uint32_t* label_out, uint32_t* parent_out);
+/* The centre schedule of the last psc_ldd / psc_cc call on g, one triple per
+ * LDD round r = 1, 2, ...: (first candidate index i, candidates offered, new
+ * centres).  Round r offers candidates hash32(1024 + i) % n for the next
+ * floor(exp(r * beta)) indices i below 1024 (src/ldd.hpp:343-373); the
+ * unlabelled ones become centres.  out holds cap triples (u32[3 * cap]);
+ * *rounds receives the number of rounds (PSC_ERR_CAPACITY if above cap). */
+int psc_ldd_rounds(psc_graph_t g, uint32_t* out, uint32_t cap, uint32_t* rounds);
 
 /* Batches of independent graphs.  No counterpart in the reference, which
  * solves one graph per call (src/scc.cpp:57-67).

@@ -660,11 +660,14 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
   uint64_t nf = 0, nf_edges = 0;
   uint32_t sampled = 0, round = 0;
   bool pull = false;
+  g->ldd_trace.clear();
   while (nf > 0 || sampled < (uint32_t)kLddSamples) {
     round++;
     if (round > n + kLddSamples + 2) return PSC_ERR_ITER_LIMIT;
     const double stepf = std::floor(std::exp((double)round * beta));
     const uint32_t work = (uint32_t)std::min<double>(stepf, (double)(kLddSamples - sampled));
+    uint32_t new_centres = 0;
+    const uint32_t first = sampled;
     if (work > 0) {
       // new centres join the frontier: appended after the nf queued vertices
       // (counter block 1 is the queue cursor) or set in the frontier bitmap
@@ -676,8 +679,10 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
           pull ? fa : nullptr, g->ctr + 1);
       sampled += work;
       PSC_TRY(read_counters(g));
+      new_centres = (uint32_t)(pull ? g->hctr[1].next : g->hctr[1].next - nf);
       nf = pull ? nf + g->hctr[1].next : g->hctr[1].next;
     }
+    g->ldd_trace.insert(g->ldd_trace.end(), {first, work, new_centres});
     if (nf == 0) continue;
     const bool want_pull = (nf + nf_edges) >= threshold;
     if (want_pull && !pull) {
@@ -891,6 +896,15 @@ extern "C" int psc_cc(psc_graph_t g, double beta, uint32_t* labels_out, uint32_t
     if (nfor) PSC_CUDA(cudaMemcpyAsync(forest_out, df, nfor * 8, cudaMemcpyDeviceToHost, g->stream));
   }
   return call_end(g);
+}
+
+extern "C" int psc_ldd_rounds(psc_graph_t g, uint32_t* out, uint32_t cap, uint32_t* rounds) {
+  if (!g || !rounds || (cap && !out)) return PSC_ERR_INVALID;
+  const uint32_t r = (uint32_t)(g->ldd_trace.size() / 3);
+  *rounds = r;
+  if (r > cap) return PSC_ERR_CAPACITY;
+  std::copy(g->ldd_trace.begin(), g->ldd_trace.end(), out);
+  return PSC_OK;
 }
 
 extern "C" int psc_ldd(psc_graph_t g, double beta, uint32_t* label_out, uint32_t* parent_out) {

@@ -115,6 +115,9 @@ struct psc_graph_s {
   int ldd_vgc_blocks = 0; // same for the LDD VGC kernel
   int le_heavy_blocks = 0; // same for the LE-list heavy-pair kernel
   bool deg_known = false;    // max_deg holds the largest out- / in-degree
+  // per LDD round of the last psc_ldd / psc_cc call: first candidate index,
+  // candidates offered, new centres (psc_ldd_rounds)
+  std::vector<uint32_t> ldd_trace;
   uint64_t max_deg[2] = {0, 0};
   uint32_t block = 0;     // threads per block of the expansion kernels (0: 256)
   // named scratch buffers, grown on demand (stream-ordered allocator)

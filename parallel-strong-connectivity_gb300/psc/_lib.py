@@ -117,6 +117,7 @@ CUDA_SIGNATURES = {
     "psc_cc": (I32, [P, D, P, P, C.POINTER(U64)]),
     "psc_bfs": (I32, [P, U32, P, C.POINTER(U32)]),
     "psc_ldd": (I32, [P, D, P, P]),
+    "psc_ldd_rounds": (I32, [P, P, U32, C.POINTER(U32)]),
     "psc_lelist": (I32, [P, P, D, P, U64, C.POINTER(U64)]),
     "psc_reach_noalloc": (I32, [P, P, P, P, U64, U64, U32, I32, P, P, C.POINTER(U32)]),
     "psc_batch_set": (I32, [P, P, U32]),

@@ -374,6 +374,20 @@ class DeviceGraph:
         check(self._lib.psc_ldd(self.h, beta, _ptr(lab), _ptr(par)), "psc_ldd")
         return lab, par
 
+    def ldd_rounds(self) -> np.ndarray:
+        """The last LDD's centre schedule: (k, 3) u32 rows (first candidate
+        index, candidates offered, new centres), one per round."""
+        r = C.c_uint32()
+        cap = 256
+        while True:
+            out = np.empty(3 * cap, np.uint32)
+            st = self._lib.psc_ldd_rounds(self.h, _ptr(out), cap, C.byref(r))
+            if st == _lib.PSC_ERR_CAPACITY:
+                cap = r.value
+                continue
+            check(st, "psc_ldd_rounds")
+            return out[: 3 * r.value].reshape(-1, 3)
+
     def bfs(self, src: int) -> np.ndarray:
         """Hop distances from src (UINT32_MAX = unreached)."""
         d = np.empty(self.n, np.uint32)

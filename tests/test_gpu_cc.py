@@ -97,3 +97,41 @@ def test_ldd_properties(kind, size, seed):
         assert par[x] in s.E[s.off[x]:s.off[x + 1]], "parent is a neighbour"
     comp = O.canon(O.cc(n, s.off, s.E))
     assert (comp[lab] == comp).all(), "clusters inside components"
+
+
+def ldd_schedule(beta, rounds):
+    """The reference's centre windows (src/ldd.hpp:343-373): round r offers
+    the next floor(exp(r * beta)) of the 1024 sampled candidates."""
+    import math
+    out, sampled = [], 0
+    for r in range(1, rounds + 1):
+        work = min(int(math.floor(math.exp(r * beta))), 1024 - sampled)
+        out.append((sampled, work))
+        sampled += work
+    return out
+
+
+@pytest.mark.parametrize("kind,size,seed", [("knn", 20000, 3), ("rmat", 14, 2), ("grid", 128, 1)])
+@pytest.mark.parametrize("beta", [0.2, 0.5])
+def test_ldd_centre_schedule(kind, size, seed, beta):
+    """LDD's centres, round by round: the candidates each round offers are the
+    reference's (hash32(1024 + i) % n in windows of floor(exp(r * beta))),
+    the first candidate is always a centre, the new centres the trace counts
+    are exactly the candidates that label themselves in the output, and every
+    other vertex is labelled by a candidate centre or (unreached) by itself."""
+    s = generated(kind, size, seed).symmetrize()
+    n = s.n
+    with psc.DeviceGraph(s) as dg:
+        lab, _ = dg.ldd(beta)
+        rows = dg.ldd_rounds()
+    assert len(rows) >= 1
+    assert [tuple(r) for r in rows[:, :2].tolist()] == ldd_schedule(beta, len(rows))
+    assert rows[:, 1].sum() == 1024
+    cand = np.array([O.lib().orc_hash32_at(1024 + i) % n for i in range(1024)], np.uint32)
+    assert lab[cand[0]] == cand[0], "the first candidate is a centre"
+    cset = np.unique(cand)
+    centres = cset[lab[cset] == cset]
+    assert rows[:, 2].sum() == len(centres)
+    assert (rows[:, 2] <= rows[:, 1]).all()
+    other = lab != np.arange(n)
+    assert np.isin(lab[other], centres).all(), "clusters belong to candidate centres"

@@ -109,3 +109,22 @@ def test_live_reference_oracle_is_the_one_pinned():
     c = ref_vectors()["rmat13_s2"]
     g = ref_graph("rmat13_s2")
     ref_check(c, "scc_s7", pyref.scc(g.n, g.off, g.E, g.in_off, g.in_E, seed=7))
+
+
+@live
+@pytest.mark.parametrize("kind,size,seed", [("knn", 20000, 3), ("rmat", 14, 2)])
+def test_live_reference_ldd_uses_the_same_candidates(kind, size, seed):
+    """The reference's LDD (src/ldd.hpp:325-417) over the stand-in's hash32
+    draws its centres from the candidates hash32(1024 + i) % n that the
+    device LDD offers (tests/test_gpu_cc.py checks the device side), and its
+    first candidate is always a centre."""
+    s = generated(kind, size, seed).symmetrize()
+    n = s.n
+    lab, rounds = pyref.ldd(n, s.off, s.E, 0.2)
+    cand = np.unique(np.array([O.lib().orc_hash32_at(1024 + i) % n for i in range(1024)],
+                              np.uint32))
+    centres = np.unique(lab[lab != np.arange(n)])
+    assert np.isin(centres, cand).all()
+    c0 = O.lib().orc_hash32_at(1024) % n
+    assert lab[c0] == c0
+    assert rounds >= 1

@@ -618,6 +618,8 @@ def run_serve(args, world, rank, local, dist) -> dict | None:
 
     def serve(rate: float | None) -> dict:
         cfg = psc.server_config(hbm_budget=SERVE["budget"], workers=args.serve_workers)
+        if args.serve_batch_edges is not None:
+            cfg.max_batch_edges = args.serve_batch_edges
         h = C.c_void_p()
         _lib.check(lib.psc_server_create(C.byref(cfg), C.byref(h)), "psc_server_create")
         arr = np.cumsum(rng.exponential(1.0 / rate, nreq)) if rate else np.zeros(nreq)
@@ -709,6 +711,9 @@ def run_serve(args, world, rank, local, dist) -> dict | None:
                             "R-MAT (16 draws per vertex), odd 2-D kNN k=5; 80 % SCC (directed), "
                             "20 % connectivity (symmetrised); Poisson arrivals",
                    "hbm_budget_gb": SERVE["budget"] / 2**30, "workers": args.serve_workers,
+                   "max_batch_edges": int(psc.server_config().max_batch_edges
+                                          if args.serve_batch_edges is None
+                                          else args.serve_batch_edges),
                    "parallelism": f"replicas{world}"},
         "sweep": sweep, "saturated": sat,
         "latency_ms": {"p50": top["p50_ms"], "p99": top["p99_ms"], "rate": top["rate"]},
@@ -999,6 +1004,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=SERVE["requests"],
                     help="requests per arrival rate of the serve workload")
     ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-batch-edges", type=int, default=None,
+                    help="serve workload: edge cap of one server batch (library default if unset)")
     ap.add_argument("--no-tune", action="store_true",
                     help="batch workload: keep the default parameters")
     ap.add_argument("--batch-count", type=int, default=4096,

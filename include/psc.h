@@ -186,9 +186,12 @@ int psc_tune_scc(psc_graph_t g, const uint64_t* seeds, uint32_t reps, psc_params
  * Submitted requests queue in arrival order.  Each of `workers` threads (one
  * CUDA stream each) takes, whenever it is free, the queued requests of the
  * kind at the head of the queue while their estimated device footprint fits
- * hbm_budget minus what running batches hold (at most max_batch requests),
- * packs them into one batch on the device, solves it with the batched path
- * and copies each member's labels to its caller.  Requests arriving while
+ * hbm_budget minus what running batches hold (at most max_batch requests
+ * and max_batch_edges edges), packs them into one batch on the device, solves
+ * it with the batched path and copies each member's labels to its caller.
+ * Batches copy their inputs to the device one after another in the order
+ * they were taken, so each reaches the device at full link speed and solves
+ * while later batches copy.  Requests arriving while
  * batches run are admitted as workers and budget free up; their work overlaps
  * the running batches.  A request larger than the whole budget is refused at
  * submission (PSC_ERR_TOO_LARGE).  Results do not depend on the mix: SCC
@@ -203,6 +206,8 @@ typedef struct {
   uint32_t max_batch;   /* requests per batch (4096) */
   double cc_beta;       /* LDD beta of connectivity requests (0.2) */
   psc_params_t scc;     /* SCC parameters; the seed comes with each request */
+  uint64_t max_batch_edges; /* edges per batch (2^28; a larger request goes
+                             * alone; 0 = no cap) */
 } psc_server_config_t;
 typedef struct {
   uint64_t submitted, completed, failed, rejected, batches;

@@ -134,6 +134,14 @@ struct psc_server_s {
   uint64_t used = 0;      // bytes admitted by running batches
   uint32_t running = 0;   // batches on the device
   int urgent_priority = 0;  // stream priority of small batches
+  // Host-to-device copies of batches go in the order the batches were taken:
+  // a batch waits for its ticket's turn, copies, then passes the turn on, so
+  // the first batches reach the device at full link speed and solve while
+  // later ones copy (instead of every batch sharing the link and finishing
+  // its copy at the same late time).
+  std::condition_variable upload_cv;
+  uint64_t next_ticket = 0;
+  uint64_t upload_turn = 0;
   bool stop = false;
   psc_server_stats_t stats{};
 };
@@ -143,12 +151,43 @@ namespace {
 
 constexpr uint64_t kUrgentEdges = 1ull << 26;
 
+// The upload turn of one batch: wait() blocks until the batch's ticket is
+// served; the turn passes to the next ticket on release() or when the batch
+// leaves run_batch without having released it.
+struct UploadTurn {
+  psc_server_s* S;
+  uint64_t ticket;
+  bool held = false, done = false;
+  void wait() {
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->upload_cv.wait(lk, [&] { return S->upload_turn == ticket; });
+    held = true;
+  }
+  void release() {
+    if (done) return;
+    if (!held) wait();
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->upload_turn++;
+    }
+    S->upload_cv.notify_all();
+    done = true;
+  }
+  ~UploadTurn() { release(); }
+};
+
+uint64_t take_ticket(psc_server_s* S) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  return S->next_ticket++;
+}
+
 // Solves one batch of requests of the same kind on a fresh handle.  When the
 // device check finds malformed requests, returns PSC_ERR_INVALID with
 // bad[k] = 1 for each of them (and nothing solved); the caller runs the rest
-// again without them.
-int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* launches,
-              std::vector<char>* bad_out) {
+// again without them.  ticket: the batch's place in the upload order.
+int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t ticket,
+              uint64_t* launches, std::vector<char>* bad_out) {
+  UploadTurn turn{S, ticket};
   const uint32_t R = (uint32_t)B.size();
   std::vector<uint64_t> vbase(R + 1, 0), ebase(R + 1, 0);
   for (uint32_t k = 0; k < R; k++) {
@@ -176,6 +215,7 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* lau
     // every SCC request brought its transpose: copy it instead of building
     bool with_t = kind == PSC_REQ_SCC;
     for (uint32_t k = 0; k < R; k++) with_t = with_t && B[k]->in_off != nullptr;
+    turn.wait();
     for (uint32_t k = 0; k < R; k++) {
       PSC_CUDA(cudaMemcpyAsync(g->off + vbase[k], B[k]->off, B[k]->n * 8, cudaMemcpyDefault, g->stream));
       if (B[k]->m)
@@ -206,7 +246,8 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t* lau
         k_validate_batch<<<vgrid, 256, 0, g->stream>>>(g->in_off, n, g->in_E, m, bases,
                                                         bases + R + 1, R, flags, any);
       PSC_CUDA(cudaGetLastError());
-      PSC_TRY(read_counters(g));
+      PSC_TRY(read_counters(g));  // the copies are done: the link is the next batch's
+      turn.release();
       if (g->hctr[2].aux0) {
         std::vector<uint64_t> hf(R);
         PSC_CUDA(cudaMemcpyAsync(hf.data(), flags, R * 8, cudaMemcpyDeviceToHost, g->stream));
@@ -270,19 +311,23 @@ bool take_batch(psc_server_s* S, std::vector<Request*>& batch, int& kind, uint64
   if (S->queue.empty()) return false;
   const uint64_t budget = S->cfg.hbm_budget;
   const uint64_t share = std::max<uint64_t>(1, budget / S->cfg.workers);
+  const uint64_t ecap = S->cfg.max_batch_edges ? S->cfg.max_batch_edges : ~0ull;
   kind = S->queue.front()->kind;
   bytes = 0;
+  uint64_t edges = 0;
   for (auto it = S->queue.begin(); it != S->queue.end() && batch.size() < S->cfg.max_batch;) {
     Request* r = *it;
     if (r->kind != kind) {
       ++it;
       continue;
     }
-    const bool fits = S->used + bytes + r->bytes <= budget && bytes + r->bytes <= share;
+    const bool fits = S->used + bytes + r->bytes <= budget && bytes + r->bytes <= share &&
+                      edges + r->m <= ecap;
     // a request larger than the share goes alone when the budget allows
     if (!fits && !(batch.empty() && (S->running == 0 || S->used + r->bytes <= budget))) break;
     batch.push_back(r);
     bytes += r->bytes;
+    edges += r->m;
     it = S->queue.erase(it);
   }
   return !batch.empty();
@@ -293,12 +338,13 @@ void worker_loop(psc_server_s* S) {
   for (;;) {
     std::vector<Request*> batch;
     int kind = 0;
-    uint64_t bytes = 0;
+    uint64_t bytes = 0, ticket = 0;
     {
       std::unique_lock<std::mutex> lk(S->mu);
       // on stop, the queue is still served before the workers leave
       S->work_cv.wait(lk, [&] { return take_batch(S, batch, kind, bytes) || S->stop; });
       if (batch.empty()) return;  // stopping with nothing to take
+      ticket = S->next_ticket++;
       S->used += bytes;
       S->running++;
       S->stats.batches++;
@@ -318,7 +364,7 @@ void worker_loop(psc_server_s* S) {
     while (!run.empty()) {
       std::vector<char> bad;
       uint64_t l = 0;
-      st = run_batch(S, run, kind, &l, &bad);
+      st = run_batch(S, run, kind, ticket, &l, &bad);
       launches += l;
       if (st != PSC_ERR_INVALID || bad.empty()) break;
       std::vector<Request*> keep;
@@ -333,6 +379,7 @@ void worker_loop(psc_server_s* S) {
       if (keep.size() == run.size()) break;  // flags without a flagged request
       run.swap(keep);
       st = PSC_OK;
+      ticket = take_ticket(S);  // the rest copies again, after the batches taken since
     }
     const auto t1 = Clock::now();
     {
@@ -370,6 +417,7 @@ extern "C" void psc_server_config_default(psc_server_config_t* c) {
   c->max_batch = 4096;
   c->cc_beta = 0.2;
   psc_params_default(&c->scc);
+  c->max_batch_edges = 1ull << 28;
 }
 
 extern "C" int psc_server_create(const psc_server_config_t* cfg, psc_server_t* out) {

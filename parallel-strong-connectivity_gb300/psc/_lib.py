@@ -67,6 +67,7 @@ class ServerConfig(C.Structure):
         ("max_batch", C.c_uint32),
         ("cc_beta", C.c_double),
         ("scc", Params),
+        ("max_batch_edges", C.c_uint64),
     ]
 
 

@@ -526,6 +526,10 @@ constexpr uint32_t kPullSolo = 64;
 #define PSC_PULL_W 4
 #endif
 constexpr int kPullW = PSC_PULL_W;  // bitmap words per warp step
+#ifndef PSC_PULL_STAGED
+#define PSC_PULL_STAGED 1
+#endif
+constexpr bool kPullStaged = PSC_PULL_STAGED != 0;  // tiles staged by bulk copies
 
 __device__ __forceinline__ bool fb_test(const uint32_t* __restrict__ fb, uint32_t x) {
   return (__ldg(&fb[x >> 5]) >> (x & 31)) & 1u;
@@ -583,97 +587,273 @@ __device__ __forceinline__ void pull_long(const uint32_t* __restrict__ B_E,
   }
 }
 
-// Pull round, W adjacent bitmap words (32 W vertices) per warp step: the
-// loads of all W words' vertices are issued together, so W dependent chains
-// (visited word, in-list range, first in-edge, frontier bit) overlap.  The
-// next round's out-edge count is left to k_pull_out_edges, off this chain.
-template <int BLOCK, int W>
-__global__ void __launch_bounds__(BLOCK)
-    k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
-                 const uint32_t* __restrict__ fb_in, uint32_t* vis, uint32_t* fb_out, uint64_t n,
-                 Counters* ctr) {
-  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
-  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
-  const uint64_t nwords = (n + 31) >> 5;
-  unsigned long long cnt = 0, scanned = 0, unvisited = 0;
-  for (uint64_t w = gw * W; w < nwords; w += nw * W) {
-    uint32_t vw[W];
-    bool t[W], f[W];
-    uint64_t b[W], e[W], j[W], lim[W];
+// One warp step of a pull round over W adjacent bitmap words (32 W vertices)
+// starting at word w: lane's vertex of word k is unvisited when t[k], with
+// in-list [b[k], e[k]).  The first in-edges of all W vertices are loaded
+// together (dense rounds often hit at once), then each unvisited vertex
+// scans alone, then the long in-lists left over are scanned by the whole
+// warp; the words' new frontier bits are written with one store each.
+template <int W>
+__device__ __forceinline__ void pull_step(uint64_t w, uint64_t nwords, const uint32_t* vw,
+                                          const bool* t, const uint64_t* b, const uint64_t* e,
+                                          const uint32_t* __restrict__ B_E,
+                                          const uint32_t* __restrict__ fb_in, uint32_t* vis,
+                                          uint32_t* fb_out, unsigned long long& cnt,
+                                          unsigned long long& scanned) {
+  const unsigned lane = lane_id();
+  bool f[W];
+  uint64_t j[W], lim[W];
+  uint32_t x[W];
 #pragma unroll
-    for (int k = 0; k < W; k++) vw[k] = w + k < nwords ? vis[w + k] : ~0u;
+  for (int k = 0; k < W; k++) {
+    lim[k] = e[k] < b[k] + kPullSolo ? e[k] : b[k] + kPullSolo;
+    j[k] = b[k];
+    x[k] = t[k] && j[k] < lim[k] ? __ldg(&B_E[j[k]]) : 0xFFFFFFFFu;
+  }
 #pragma unroll
-    for (int k = 0; k < W; k++) {
-      const uint64_t v = (w + k) * 32 + lane;
-      t[k] = v < n && !((vw[k] >> lane) & 1u);
-      b[k] = e[k] = 0;
-      if (t[k]) {
-        b[k] = B_off[v];
-        e[k] = B_off[v + 1];
-      }
-      unvisited += t[k] ? 1 : 0;
-    }
-    // the first in-edge of all W vertices together (dense rounds often hit
-    // at once)
-    uint32_t x[W];
+  for (int k = 0; k < W; k++) {
+    f[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
+    if (t[k] && j[k] < lim[k]) j[k]++;
+  }
 #pragma unroll
-    for (int k = 0; k < W; k++) {
-      lim[k] = e[k] < b[k] + kPullSolo ? e[k] : b[k] + kPullSolo;
-      j[k] = b[k];
-      x[k] = j[k] < lim[k] ? __ldg(&B_E[j[k]]) : 0xFFFFFFFFu;
-    }
+  for (int k = 0; k < W; k++)
+    if (t[k] && !f[k]) f[k] = pull_scan(B_E, fb_in, j[k], lim[k]);
 #pragma unroll
-    for (int k = 0; k < W; k++) {
-      f[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
-      if (j[k] < lim[k]) j[k]++;
-    }
+  for (int k = 0; k < W; k++)
+    if (t[k]) scanned += j[k] - b[k];
 #pragma unroll
-    for (int k = 0; k < W; k++)
-      if (!f[k]) f[k] = pull_scan(B_E, fb_in, j[k], lim[k]);
+  for (int k = 0; k < W; k++)
+    pull_long(B_E, fb_in, __ballot_sync(kFull, t[k] && !f[k] && j[k] < e[k]), j[k], e[k], f[k],
+              scanned);
 #pragma unroll
-    for (int k = 0; k < W; k++)
-      if (t[k]) scanned += j[k] - b[k];
-#pragma unroll
-    for (int k = 0; k < W; k++)
-      pull_long(B_E, fb_in, __ballot_sync(kFull, t[k] && !f[k] && j[k] < e[k]), j[k], e[k], f[k],
-                scanned);
-#pragma unroll
-    for (int k = 0; k < W; k++) {
-      const uint32_t mk = __ballot_sync(kFull, f[k]);
-      if (lane == 0 && w + k < nwords) {
-        fb_out[w + k] = mk;
-        if (mk) vis[w + k] = vw[k] | mk;
-        cnt += __popc(mk);
-      }
+  for (int k = 0; k < W; k++) {
+    const uint32_t mk = __ballot_sync(kFull, f[k]);
+    if (lane == 0 && w + k < nwords) {
+      fb_out[w + k] = mk;
+      if (mk) vis[w + k] = vw[k] | mk;
+      cnt += __popc(mk);
     }
   }
+}
+
+__device__ __forceinline__ void flush_pull_counters(Counters* ctr, unsigned long long cnt,
+                                                    unsigned long long scanned,
+                                                    unsigned long long unvisited) {
   scanned = warp_sum(scanned);
   unvisited = warp_sum(unvisited);
-  if (lane == 0) {
+  if (lane_id() == 0) {
     if (cnt) atomicAdd(&ctr->next, cnt);
     if (scanned) atomicAdd(&ctr->edges, scanned);
     if (unvisited) atomicAdd(&ctr->unvisited, unvisited);
   }
 }
 
-// Out-edges of the frontier a pull round left in fb (ctr->next vertices),
-// for the next round's push / pull choice (REACH::judge, src/reach.hpp:86-112).
-// A small frontier (under kPullExactBelow) gets its exact degree sum over the
-// whole grid, as the reference packs it and sums its degrees; a larger one an
-// estimate from the degrees of 50 frontier vertices met by hashed probes
-// hash32(seed + i) % n, i = 1, 2, ..., times the frontier size
-// (REACH::dense_sample, :192-206), done by the first warp of the grid (at
-// most kSampleProbes probes; no hit gives 0).  Writes ctr->next_edges.
+// A warp's W words read from global memory: visited words and in-list ranges.
+template <int W>
+__device__ __forceinline__ void pull_load_global(uint64_t w, uint64_t nwords, uint64_t n,
+                                                 const uint64_t* __restrict__ B_off,
+                                                 const uint32_t* vis, uint32_t* vw, bool* t,
+                                                 uint64_t* b, uint64_t* e,
+                                                 unsigned long long& unvisited) {
+  const unsigned lane = lane_id();
+#pragma unroll
+  for (int k = 0; k < W; k++) vw[k] = w + k < nwords ? vis[w + k] : ~0u;
+#pragma unroll
+  for (int k = 0; k < W; k++) {
+    const uint64_t v = (w + k) * 32 + lane;
+    t[k] = v < n && !((vw[k] >> lane) & 1u);
+    b[k] = e[k] = 0;
+    if (t[k]) {
+      b[k] = B_off[v];
+      e[k] = B_off[v + 1];
+    }
+    unvisited += t[k] ? 1 : 0;
+  }
+}
+
+// Pull round reading the visited words and in-list offsets from global
+// memory: W words per warp step, so W dependent chains (visited word,
+// in-list range, first in-edge, frontier bit) overlap.  The next round's
+// out-edge count is left to k_pull_out_edges, off this chain.
+template <int BLOCK, int W>
+__global__ void __launch_bounds__(BLOCK)
+    k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
+                 const uint32_t* __restrict__ fb_in, uint32_t* vis, uint32_t* fb_out, uint64_t n,
+                 Counters* ctr) {
+  const unsigned wid = threadIdx.x >> 5;
+  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
+  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  const uint64_t nwords = (n + 31) >> 5;
+  unsigned long long cnt = 0, scanned = 0, unvisited = 0;
+  for (uint64_t w = gw * W; w < nwords; w += nw * W) {
+    uint32_t vw[W];
+    bool t[W];
+    uint64_t b[W], e[W];
+    pull_load_global<W>(w, nwords, n, B_off, vis, vw, t, b, e, unvisited);
+    pull_step<W>(w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
+  }
+  flush_pull_counters(ctr, cnt, scanned, unvisited);
+}
+
+// ---------------------------------------------------------------------------
+// Bulk asynchronous copies into shared memory (cp.async.bulk, the 1-D form of
+// the tensor memory accelerator's copies) completing on an mbarrier.  Every
+// wait is bounded: past kStageSpin polls it gives up and the kernel reports
+// the failure through its counters instead of waiting on.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kStageSpin = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kStageSpin; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Pull round with staged tiles: a block's tiles of TV = 32 W (BLOCK / 32)
+// consecutive vertices are taken in grid-stride order; the visited words and
+// the in-list offsets of the tile after next are copied into one of two
+// shared-memory buffers while the current one is worked on, so the loads
+// left on a warp's dependent chain are the first in-edge and the frontier
+// bit.  A tile is staged when its copy stays inside the arrays (offsets
+// [v0, v0 + TV + 2) with v0 + TV + 1 <= n); the last tiles are read from
+// global memory like k_reach_pull.  A copy that does not arrive within the
+// bounded wait sets ctr->aux1 and the block stops (the host reports it).
+template <int BLOCK, int W>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
+    k_reach_pull_staged(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
+                        const uint32_t* __restrict__ fb_in, uint32_t* vis, uint32_t* fb_out,
+                        uint64_t n, Counters* ctr) {
+  constexpr uint32_t NW = BLOCK / 32;
+  constexpr uint32_t TV = NW * 32 * W;  // vertices per tile
+  constexpr uint32_t TW = TV / 32;      // visited words per tile
+  constexpr uint32_t OFF_BYTES = (TV + 2) * 8;
+  constexpr uint32_t VIS_BYTES = TW * 4;
+  static_assert(OFF_BYTES % 16 == 0 && VIS_BYTES % 16 == 0, "bulk copies of 16-byte multiples");
+  __shared__ __align__(128) uint64_t soff[2][TV + 2];
+  __shared__ __align__(128) uint32_t svis[2][TW];
+  __shared__ __align__(8) uint64_t bar[2];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const uint64_t nwords = (n + 31) >> 5;
+  const uint64_t ntiles = (n + TV - 1) / TV;
+  auto staged = [&](uint64_t tile) { return tile * TV + TV + 1 <= n; };
+  auto issue = [&](uint64_t tile, int buf) {  // one thread
+    mbar_expect_tx(&bar[buf], OFF_BYTES + VIS_BYTES);
+    bulk_copy_g2s(soff[buf], B_off + tile * TV, OFF_BYTES, &bar[buf]);
+    bulk_copy_g2s(svis[buf], vis + tile * TW, VIS_BYTES, &bar[buf]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // bit b: the phase parity to wait for / a copy in flight, of buffer b
+  uint32_t parity = 0, pending = 0;
+  const uint64_t t0 = blockIdx.x, tstep = gridDim.x;
+  for (int bb = 0; bb < 2; bb++) {
+    const uint64_t tile = t0 + bb * tstep;
+    if (tile < ntiles && staged(tile)) {
+      if (threadIdx.x == 0) issue(tile, bb);
+      pending |= 1u << bb;
+    }
+  }
+  unsigned long long cnt = 0, scanned = 0, unvisited = 0;
+  bool failed = false;
+  int buf = 0;
+  for (uint64_t tile = t0; tile < ntiles; tile += tstep, buf ^= 1) {
+    const uint64_t w = tile * TW + wid * W;  // this warp's first word
+    uint32_t vw[W];
+    bool t[W];
+    uint64_t b[W], e[W];
+    if ((pending >> buf) & 1u) {
+      // every thread waits for the tile; giving up is decided block-wide
+      const bool ok = mbar_wait_bounded(&bar[buf], (parity >> buf) & 1u);
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      parity ^= 1u << buf;
+      pending &= ~(1u << buf);
+#pragma unroll
+      for (int k = 0; k < W; k++) {
+        const uint32_t li = (wid * W + k) * 32 + lane;
+        vw[k] = svis[buf][wid * W + k];
+        t[k] = !((vw[k] >> lane) & 1u);
+        b[k] = e[k] = 0;
+        if (t[k]) {
+          b[k] = soff[buf][li];
+          e[k] = soff[buf][li + 1];
+        }
+        unvisited += t[k] ? 1 : 0;
+      }
+    } else {
+      pull_load_global<W>(w, nwords, n, B_off, vis, vw, t, b, e, unvisited);
+    }
+    pull_step<W>(w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
+    // every warp is done with this buffer before the copy of the tile after
+    // next lands in it
+    __syncthreads();
+    const uint64_t nt = tile + 2 * tstep;
+    if (nt < ntiles && staged(nt)) {
+      if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(nt, buf);
+      }
+      pending |= 1u << buf;
+    }
+  }
+  if (failed) {
+    // the copies still in flight land before the block's shared memory goes
+    if (pending & 1u) mbar_wait_bounded(&bar[0], parity & 1u);
+    if (pending & 2u) mbar_wait_bounded(&bar[1], (parity >> 1) & 1u);
+    if (lane == 0) atomicOr(&ctr->aux1, 1ull);
+  }
+  flush_pull_counters(ctr, cnt, scanned, unvisited);
+}
+
 // A pull round's grid: the resident blocks of the kernel (a grid-stride loop
 // covers the rest), fewer when the bitmap has fewer warp steps than that.
-template <int BLOCK>
+template <int BLOCK, bool STAGED = false>
 static unsigned pull_grid(int num_sms, uint64_t nwords) {
   static int per_sm = [] {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_reach_pull<BLOCK, kPullW>, BLOCK, 0) !=
-            cudaSuccess ||
-        b < 1) {
+    cudaError_t e =
+        STAGED ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                     &b, k_reach_pull_staged<BLOCK, kPullW>, BLOCK, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_reach_pull<BLOCK, kPullW>,
+                                                               BLOCK, 0);
+    if (e != cudaSuccess || b < 1) {
       cudaGetLastError();
       b = 1;
     }
@@ -684,6 +864,8 @@ static unsigned pull_grid(int num_sms, uint64_t nwords) {
   const uint64_t cap = (uint64_t)num_sms * per_sm;
   return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
 }
+
+constexpr uint64_t kPullStagedTile = (uint64_t)kReachBlock * kPullW;  // vertices of a staged tile
 
 constexpr uint64_t kPullExactBelow = 1u << 14;
 constexpr uint32_t kSampleProbes = 32 * 64;
@@ -1093,9 +1275,17 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
               B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
           break;
         default:
-          k_reach_pull<kReachBlock, kPullW>
-              <<<pull_grid<kReachBlock>(g->num_sms, nwords), kReachBlock, 0, g->stream>>>(
-                  B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
+          // staged tiles when at least one tile fits inside the arrays and
+          // they are 16-byte aligned (bulk copies)
+          if (kPullStaged && n >= kPullStagedTile + 1 && ((uintptr_t)B_off & 15) == 0 &&
+              ((uintptr_t)s.vis & 15) == 0)
+            k_reach_pull_staged<kReachBlock, kPullW>
+                <<<pull_grid<kReachBlock, true>(g->num_sms, nwords), kReachBlock, 0, g->stream>>>(
+                    B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
+          else
+            k_reach_pull<kReachBlock, kPullW>
+                <<<pull_grid<kReachBlock>(g->num_sms, nwords), kReachBlock, 0, g->stream>>>(
+                    B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
       }
       k_pull_out_edges<<<grid_for(g, nwords, 256), 256, 0, g->stream>>>(
           fbo, A_off, n, hash32((uint32_t)s.rounds), g->ctr + s.cset);
@@ -1141,6 +1331,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       Side& s = sides[k];
       if (mode[k] == M_NONE) continue;
       const Counters& c = g->hctr[s.cset];
+      if (mode[k] == M_PULL && c.aux1) return PSC_ERR_ITER_LIMIT;  // a staged copy never came
       if (g->profiling) {
         // algorithmic bytes: 16 per adjacency range read, 4 + 1 per edge
         // (target id, visited flag), 5 per new frontier vertex; pull: 16 per

@@ -18,6 +18,9 @@ int batch_attach(psc_graph_s* g, const uint64_t* vbase, uint32_t num_graphs, boo
 int call_begin(psc_graph_s* g);
 int call_end(psc_graph_s* g);
 
+// g->max_deg (largest out- / in-degree), computed once per handle.
+int ensure_max_degrees(psc_graph_s* g);
+
 // Builds in_off/in_E from off/E on the device (in-lists sorted by source).
 int build_transpose(psc_graph_s* g);
 // Replaces off/E by their symmetrisation on the device (both directions,
@@ -53,9 +56,20 @@ struct MsResult {
   uint64_t cap = 0;  // table capacity (power of two)
   uint64_t ne = 0;   // entries
 };
+// Asynchronous start of a batch (MsAsync given): the pivot count is read on
+// the device at *nf_dev (n_front is only its upper bound), so the seeds and
+// the first sub-round are launched without waiting for the compaction that
+// wrote front.  On return n_front holds the pivot count.  (The partition
+// cannot start early: later sub-rounds test subproblems on the labels it
+// writes.)
+struct MsAsync {
+  const unsigned long long* nf_dev = nullptr;
+  uint64_t n_front = 0;
+};
 int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t label_offset,
             const uint64_t* labels, const psc_params_t* p, const uint64_t prev_ne[2],
-            MsResult out[2], const uint32_t* front_labels = nullptr, uint64_t vgc_max = 0);
+            MsResult out[2], const uint32_t* front_labels = nullptr, uint64_t vgc_max = 0,
+            MsAsync* async = nullptr);
 
 // Partition of one batch (src/scc.hpp:437-464): (v, l) in both tables left by
 // ms_pair -> labels[v] = max(l | TOP), else max(l).

@@ -54,6 +54,9 @@ struct MsSide {
   uint32_t* hflag;
   Counters* ctr;
   uint32_t vgc_budget;  // new pairs one VGC local search may insert
+  // when set, the frontier size is read here instead of nin (the first
+  // sub-round of a batch started without waiting for its pivot count)
+  const unsigned long long* nin_dev;
 };
 
 constexpr int kMsHeavyK = 4;  // heavy pairs: edges in flight per lane
@@ -81,7 +84,8 @@ struct MsSrc {
 
 __global__ void k_ms_seed(const uint32_t* __restrict__ front, uint64_t nf, uint64_t label_offset,
                           const uint32_t* __restrict__ front_labels, unsigned long long* T,
-                          uint64_t mask, uint64_t* F) {
+                          uint64_t mask, uint64_t* F, const unsigned long long* nf_dev) {
+  if (nf_dev) nf = *nf_dev;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t lab = front_labels ? front_labels[i] : (uint32_t)(label_offset + i);
@@ -274,6 +278,8 @@ __device__ __forceinline__ void flush_ms_counters(Counters* c0, Counters* c1,
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, (768 / BLOCK) > 0 ? (768 / BLOCK) : 1)
     k_ms_expand(MsSide s0, MsSide s1, const uint64_t* __restrict__ labels) {
+  if (s0.nin_dev) s0.nin = *s0.nin_dev;
+  if (s1.nin_dev) s1.nin = *s1.nin_dev;
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ MsSrc ssrc[BLOCK / 32];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -430,6 +436,8 @@ __device__ __forceinline__ void ms_vgc_place(uint32_t tm, const uint32_t* w, con
 template <int BLOCK, int QCAP>
 __global__ void __launch_bounds__(BLOCK)
     k_ms_vgc(MsSide s0, MsSide s1, const uint64_t* __restrict__ labels, uint32_t tau) {
+  if (s0.nin_dev) s0.nin = *s0.nin_dev;
+  if (s1.nin_dev) s1.nin = *s1.nin_dev;
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ MsQEnt sq[BLOCK / 32][QCAP];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -732,6 +740,7 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
   r.Fheavy = (uint64_t*)g->bufs[s.h_slot].p;
   r.hflag = (uint32_t*)g->bufs[s.f_slot].p;
   r.ctr = g->ctr + s.cset;
+  r.nin_dev = nullptr;
   // VGC local searches share the room left below half load, so one
   // sub-round cannot fill the table
   const uint64_t room = s.cap / 2 > s.ne ? s.cap / 2 - s.ne : 0;
@@ -744,7 +753,7 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
 
 int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t label_offset,
             const uint64_t* labels, const psc_params_t* p, const uint64_t prev_ne[2],
-            MsResult out[2], const uint32_t* front_labels, uint64_t vgc_max) {
+            MsResult out[2], const uint32_t* front_labels, uint64_t vgc_max, MsAsync* async) {
   // heavy-list fields: < 2^24 pairs (m / kHeavyDeg), first chunks < 2^31
   if (g->m >> 36) return PSC_ERR_TOO_LARGE;
   const uint32_t tau = p->tau ? p->tau : 512;
@@ -770,10 +779,17 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       ps.bytes = 20.0 * n_front;
       k_ms_seed<<<grid_for(g, n_front, 256), 256, 0, g->stream>>>(
           front, n_front, label_offset, front_labels, (unsigned long long*)g->bufs[s.t_slot].p,
-          s.cap - 1,
-          (uint64_t*)g->bufs[s.a_slot].p);
+          s.cap - 1, (uint64_t*)g->bufs[s.a_slot].p, async ? async->nf_dev : nullptr);
     }
     s.nf = s.ne = n_front;
+  }
+  // asynchronous start: the first sub-round runs on the device's pivot count
+  // and the heavy walk follows it whenever some vertex could be heavy
+  bool first_async = async && async->nf_dev;
+  bool heavy_possible = false;
+  if (first_async) {
+    PSC_TRY(ensure_max_degrees(g));
+    heavy_possible = g->max_deg[0] > kHeavyDeg || g->max_deg[1] > kHeavyDeg;
   }
   for (;;) {
     bool any = false;
@@ -802,6 +818,9 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
     }
     if (!any) break;
     PSC_TRY(zero_counters(g));
+    if (first_async)  // the pivot count comes back with the counters (staging set 3)
+      PSC_CUDA(cudaMemcpyAsync(&g->ctr[3].aux0, async->nf_dev, sizeof(unsigned long long),
+                               cudaMemcpyDeviceToDevice, g->stream));
     MsSide vg[2] = {}, ex[2] = {}, hv[2] = {};
     int nv = 0, ne = 0, nh = 0;
     uint64_t v_items = 0, e_items = 0;
@@ -809,6 +828,7 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
     for (int k = 0; k < 2; k++) {
       if (st[k].nf == 0) continue;
       MsSide a = ms_args(g, st[k]);
+      if (first_async) a.nin_dev = async->nf_dev;
       is_vgc[k] = local && st[k].nf <= vgc_limit;
       if (is_vgc[k]) {
         vg[nv++] = a;
@@ -848,10 +868,30 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       }
     }
     PSC_CUDA(cudaGetLastError());
+    if (first_async && heavy_possible) {  // returns at once when no pair was listed
+      ProfScope ps(g, F_HEAVY);
+      k_ms_heavy<kMsBlock><<<g->num_sms * 4, kMsBlock, 0, g->stream>>>(hv[0], hv[1], labels);
+    }
     PSC_TRY(read_counters(g));
+    if (first_async) {
+      // the pivot count replaces its upper bound
+      const uint64_t nf0 = g->hctr[3].aux0;
+      async->n_front = nf0;
+      for (auto& s : st) {
+        s.ne = s.ne - s.nf + nf0;
+        s.nf = nf0;
+      }
+      if (g->profiling && heavy_possible)
+        for (int k = 0; k < 2; k++) {
+          const Counters& c = g->hctr[st[k].cset];
+          g->prof[F_HEAVY].bytes +=
+              28.0 * (c.heavy >> kPackShift) + 12.0 * c.heavy_edges + 8.0 * c.heavy_probes;
+        }
+    }
     // Heavy pairs are rare: the grid-wide walk is launched only for a round
     // that queued some, then the counters are read again.
-    if ((st[0].nf && g->hctr[st[0].cset].heavy) || (st[1].nf && g->hctr[st[1].cset].heavy)) {
+    if (!first_async &&
+        ((st[0].nf && g->hctr[st[0].cset].heavy) || (st[1].nf && g->hctr[st[1].cset].heavy))) {
       {
         ProfScope ps(g, F_HEAVY);
         k_ms_heavy<kMsBlock><<<g->num_sms * 4, kMsBlock, 0, g->stream>>>(hv[0], hv[1], labels);
@@ -897,7 +937,9 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       std::swap(g->bufs[s.a_slot], g->bufs[s.b_slot]);
       s.nf = c.next;
     }
+    first_async = false;
   }
+  if (async && !async->nf_dev) async->n_front = n_front;
   for (int k = 0; k < 2; k++) {
     out[k].cap = st[k].cap;
     out[k].ne = st[k].ne;

@@ -1005,7 +1005,7 @@ __global__ void k_max_degrees(const uint64_t* __restrict__ off, const uint64_t* 
 
 // Once per handle (the graph does not change): max_deg for the heavy-vertex
 // check of chained rounds.
-static int ensure_max_degrees(psc_graph_s* g) {
+int max_degrees_once(psc_graph_s* g) {
   if (g->deg_known) return PSC_OK;
   unsigned long long* d = &g->ctr[2].aux0;  // aux0, aux1 of the staging set
   PSC_CUDA(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), g->stream));
@@ -1066,6 +1066,8 @@ Side make_side(bool backward, uint32_t* vis, int second) {
 
 }  // namespace
 
+int ensure_max_degrees(psc_graph_s* g) { return max_degrees_once(g); }
+
 // Runs the searches of `ns` sides (1 or 2) to completion.  Side k starts from
 // srcs[k], or, when d_srcs is given, every side starts from the n_dsrc device
 // sources d_srcs.
@@ -1125,7 +1127,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
                  2 * s.nf <= 3 * s.prev_nf && 3 * (s.nf + s.nf_edges) < threshold;
       }
       if (na > 0 && steady) {
-        PSC_TRY(ensure_max_degrees(g));
+        PSC_TRY(max_degrees_once(g));
         bool heavy_possible = false;  // some active direction has a vertex above kHeavyDeg
         for (int a = 0; a < na; a++)
           heavy_possible |= g->max_deg[sides[act[a]].backward ? 1 : 0] > kHeavyDeg;

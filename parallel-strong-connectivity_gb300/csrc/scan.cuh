@@ -207,9 +207,13 @@ int scan_emit(psc_graph_s* g, uint64_t n, Value value, Emit emit, uint64_t* tota
 }
 
 // scan_emit for a value that is 0 or 1 (a selection); see the file comment.
+// total_dev (optional): receives the device address of the total (valid
+// until the next scan on this handle), for kernels that read the count
+// without a wait on the host.
 template <class Value, class Emit>
 int scan_emit_flags(psc_graph_s* g, uint64_t n, Value value, Emit emit, uint64_t* total,
-                    int fam = F_COMPACT, double item_bytes = 0, double sel_bytes = 0) {
+                    int fam = F_COMPACT, double item_bytes = 0, double sel_bytes = 0,
+                    const unsigned long long** total_dev = nullptr) {
   if (n == 0) {
     if (total) *total = 0;
     return PSC_OK;
@@ -232,6 +236,7 @@ int scan_emit_flags(psc_graph_s* g, uint64_t n, Value value, Emit emit, uint64_t
     k_tile_emit<<<(unsigned)ntiles, kScanBlock, 0, g->stream>>>(BitValue{bits}, emit, n, ts);
   }
   PSC_CUDA(cudaGetLastError());
+  if (total_dev) *total_dev = (const unsigned long long*)(ts + ntiles);
   if (total) {
     PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux0, ts + ntiles, sizeof(uint64_t), cudaMemcpyDeviceToHost,
                              g->stream));

@@ -167,6 +167,11 @@ int scc_partition(psc_graph_s* g, const MsResult res[2], uint64_t* labels) {
   return PSC_OK;
 }
 
+// Batches of at most this many candidate pivots start asynchronously (see
+// the batch loop below); larger ones wait for their pivot count, which sizes
+// their tables.
+constexpr uint64_t kAsyncBatch = 1u << 16;
+
 static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
   const uint64_t n = g->n;
   const unsigned tb = 256;
@@ -227,15 +232,29 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
       step_size = (uint64_t)std::ceil((double)step_size * p->beta);
       if (step_size > n_remaining) step_size = n_remaining;
       if (step_size == 0) step_size = 1;
+      // Small batches start without waiting for their pivot count: the
+      // compaction's total is read on the device by the seeds and the first
+      // sub-round, so the batch waits on the host once per sub-round only.
+      const bool async = vs_size <= kAsyncBatch;
       uint64_t nf = 0;
+      const unsigned long long* nf_dev = nullptr;
       PSC_TRY(scan_emit_flags(g, vs_size, NotDoneAt{centers, labels, cur_offset},
-                        CopyAt{centers, front, cur_offset}, &nf, F_COMPACT, 12.0, 4.0));
+                              CopyAt{centers, front, cur_offset}, async ? nullptr : &nf,
+                              F_COMPACT, 12.0, 4.0, async ? &nf_dev : nullptr));
       cur_offset = end;
-      if (nf == 0) continue;
-      g->stats.batches++;
+      if (!async && nf == 0) continue;
       MsResult res[2];
       const uint64_t prev[2] = {out_ne, in_ne};
-      PSC_TRY(ms_pair(g, front, nf, label_offset, labels, p, prev, res));
+      if (async) {
+        MsAsync as;
+        as.nf_dev = nf_dev;
+        PSC_TRY(ms_pair(g, front, vs_size, label_offset, labels, p, prev, res, nullptr, 0, &as));
+        nf = as.n_front;
+        if (nf == 0) continue;
+      } else {
+        PSC_TRY(ms_pair(g, front, nf, label_offset, labels, p, prev, res));
+      }
+      g->stats.batches++;
       label_offset += nf;
       PSC_TRY(scc_partition(g, res, labels));
       out_ne = res[0].ne;

@@ -753,9 +753,12 @@ def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
                       "restatement of src/scc.hpp)"}
 
 
-# DRAM bytes (read + write) of one launch of a workload's dominant kernel from
-# one ncu capture of the same command (profiles/k_reach_vgc_knn1e7.md).
-NCU_TRAFFIC = {("scc_knn", "reach_vgc"): 91.9e6}
+# DRAM bytes (read + write) per launch of a workload's dominant kernel family:
+# dram__bytes_read.sum + dram__bytes_write.sum averaged over the family's
+# launches in one ncu capture (a single pass) of
+# `python bench.py --ncu-step --workload W` on the current kernels.  A
+# workload without a capture of its current dominant kernel reports null.
+NCU_TRAFFIC: dict = {}
 
 
 def roofline_of(prof: dict, steps: int, workload: str = "") -> dict:

@@ -127,3 +127,22 @@ def test_server_rejects_bad_requests():
             srv.wait(12345)      # unknown id
         lab, _ = srv.wait(srv.submit(g, SCC, 1))
         assert len(np.unique(lab)) == 3
+
+
+def test_server_edge_cap_splits_batches():
+    """max_batch_edges: a batch holds at most that many edges (a larger
+    request goes alone), and results stay those of solo solves."""
+    reqs = stream(24, seed0=700)
+    cap = max(g.m for g, _, _ in reqs) // 2
+    with psc.Server(workers=2, max_batch_edges=cap) as srv:
+        ids = [srv.submit(g, kind, seed, with_transpose=(k % 2 == 0))
+               for k, (g, kind, seed) in enumerate(reqs)]
+        infos = []
+        for rid, (g, kind, seed) in zip(ids, reqs):
+            lab, info = srv.wait(rid)
+            assert info.status == 0
+            check_result(g, kind, seed, lab)
+            infos.append((info.batch_size, g.m))
+    # a request above the cap was solved alone
+    assert all(bs == 1 for bs, m in infos if m > cap)
+    assert psc.server_config().max_batch_edges == 1 << 28

@@ -153,14 +153,19 @@ constexpr uint64_t kUrgentEdges = 1ull << 26;
 
 // The upload turn of one batch: wait() blocks until the batch's ticket is
 // served; the turn passes to the next ticket on release() or when the batch
-// leaves run_batch without having released it.
+// leaves run_batch without having released it.  The wait is bounded
+// (kTurnWait): a batch whose turn does not come copies anyway (the order is a
+// schedule, not a correctness condition) and then passes the turn on only if
+// it is still its own, so no batch can block the others for good.
+constexpr std::chrono::seconds kTurnWait{30};
+
 struct UploadTurn {
   psc_server_s* S;
   uint64_t ticket;
   bool held = false, done = false;
   void wait() {
     std::unique_lock<std::mutex> lk(S->mu);
-    S->upload_cv.wait(lk, [&] { return S->upload_turn == ticket; });
+    S->upload_cv.wait_for(lk, kTurnWait, [&] { return S->upload_turn >= ticket; });
     held = true;
   }
   void release() {
@@ -168,7 +173,7 @@ struct UploadTurn {
     if (!held) wait();
     {
       std::lock_guard<std::mutex> lk(S->mu);
-      S->upload_turn++;
+      if (S->upload_turn <= ticket) S->upload_turn = ticket + 1;
     }
     S->upload_cv.notify_all();
     done = true;
@@ -379,7 +384,9 @@ void worker_loop(psc_server_s* S) {
       if (keep.size() == run.size()) break;  // flags without a flagged request
       run.swap(keep);
       st = PSC_OK;
-      ticket = take_ticket(S);  // the rest copies again, after the batches taken since
+      // the rest copies again, after the batches taken since (a ticket is
+      // drawn only for a run that follows: every ticket drawn must be served)
+      if (!run.empty()) ticket = take_ticket(S);
     }
     const auto t1 = Clock::now();
     {

@@ -20,9 +20,6 @@ int call_end(psc_graph_s* g);
 
 // g->max_deg (largest out- / in-degree), computed once per handle.
 int ensure_max_degrees(psc_graph_s* g);
-// Adjacency records (VRec) of the out-lists (backward = false) or in-lists,
-// built once per handle; *out = null when records are switched off.
-int vgc_records(psc_graph_s* g, bool backward, const VRec** out);
 
 // Builds in_off/in_E from off/E on the device (in-lists sorted by source).
 int build_transpose(psc_graph_s* g);

@@ -57,8 +57,6 @@ struct MsSide {
   // when set, the frontier size is read here instead of nin (the first
   // sub-round of a batch started without waiting for its pivot count)
   const unsigned long long* nin_dev;
-  // VGC sub-rounds: adjacency records of this direction (null: off / E)
-  const VRec* rec;
 };
 
 constexpr int kMsHeavyK = 4;  // heavy pairs: edges in flight per lane
@@ -349,7 +347,6 @@ template <int K, bool ADJ = true>
 __device__ __forceinline__ uint32_t ms_vgc_claim(const uint32_t* w, uint64_t* vb, uint64_t* ve,
                                                  uint64_t sub, uint32_t lab,
                                                  const uint64_t* __restrict__ off,
-                                                 const VRec* __restrict__ rec,
                                                  const uint64_t* __restrict__ labels,
                                                  unsigned long long* T, uint64_t mask,
                                                  uint32_t& probes, bool& failed) {
@@ -360,12 +357,7 @@ __device__ __forceinline__ uint32_t ms_vgc_claim(const uint32_t* w, uint64_t* vb
     vb[k] = ve[k] = 0;
     if (w[k] != 0xFFFFFFFFu) {
       const uint64_t lw = __ldg(&labels[w[k]]);
-      if (ADJ && rec) {
-        // the record's sector also holds the inline targets the next wave reads
-        const uint4 r = __ldg(reinterpret_cast<const uint4*>(rec + w[k]));
-        vb[k] = (uint64_t)r.x | ((uint64_t)r.y << 32);
-        ve[k] = vb[k] + r.z;
-      } else if (ADJ) {
+      if (ADJ) {
         vb[k] = __ldg(&off[w[k]]);
         ve[k] = __ldg(&off[w[k] + 1]);
       }
@@ -448,7 +440,6 @@ __global__ void __launch_bounds__(BLOCK)
   if (s1.nin_dev) s1.nin = *s1.nin_dev;
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ MsQEnt sq[BLOCK / 32][QCAP];
-  __shared__ uint32_t sv[BLOCK / 32][32];  // the wave's vertices (their records)
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
@@ -491,8 +482,8 @@ __global__ void __launch_bounds__(BLOCK)
           w[k] = e < ue ? __ldg(&S.E[e]) : 0xFFFFFFFFu;
         }
         bool fk = false;
-        const uint32_t tm = ms_vgc_claim<kMsK, false>(w, vb, ve, sub, lab, S.off, S.rec, labels,
-                                                      S.T, S.mask, probes, fk);
+        const uint32_t tm = ms_vgc_claim<kMsK, false>(w, vb, ve, sub, lab, S.off, labels, S.T,
+                                                      S.mask, probes, fk);
         failed |= fk;
         (sd ? in1 : in0) += __popc(tm);
 #pragma unroll
@@ -540,7 +531,6 @@ __global__ void __launch_bounds__(BLOCK)
       const uint32_t total = __shfl_sync(kFull, incl, 31);
       sm[wid].excl[lane] = incl - deg;
       sm[wid].beg[lane] = beg;
-      sv[wid][lane] = x;
       __syncwarp();
       for (uint32_t base = 0; base < total; base += 32 * kMsK) {
         uint32_t w[kMsK];
@@ -561,14 +551,12 @@ __global__ void __launch_bounds__(BLOCK)
                 hi = mid - 1;
             }
             sl[k] = lo;
-            const uint32_t j = gi - sm[wid].excl[lo];
-            w[k] = S.rec && j < (uint32_t)kRecEdges ? __ldg(&S.rec[sv[wid][lo]].e[j])
-                                                     : __ldg(&S.E[sm[wid].beg[lo] + j]);
+            w[k] = __ldg(&S.E[sm[wid].beg[lo] + (gi - sm[wid].excl[lo])]);
           }
         }
         bool fk = false;
-        const uint32_t tm = ms_vgc_claim<kMsK>(w, vb, ve, sub, lab, S.off, S.rec, labels, S.T,
-                                               S.mask, probes, fk);
+        const uint32_t tm = ms_vgc_claim<kMsK>(w, vb, ve, sub, lab, S.off, labels, S.T, S.mask,
+                                               probes, fk);
         // a failure is charged to the source lane of the failed edge
         if (fk) {
 #pragma unroll
@@ -753,7 +741,6 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
   r.hflag = (uint32_t*)g->bufs[s.f_slot].p;
   r.ctr = g->ctr + s.cset;
   r.nin_dev = nullptr;
-  r.rec = nullptr;
   // VGC local searches share the room left below half load, so one
   // sub-round cannot fill the table
   const uint64_t room = s.cap / 2 > s.ne ? s.cap / 2 - s.ne : 0;
@@ -844,7 +831,6 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       if (first_async) a.nin_dev = async->nf_dev;
       is_vgc[k] = local && st[k].nf <= vgc_limit;
       if (is_vgc[k]) {
-        PSC_TRY(vgc_records(g, st[k].backward, &a.rec));
         vg[nv++] = a;
         v_items += st[k].nf;
       } else {

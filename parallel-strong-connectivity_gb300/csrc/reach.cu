@@ -1127,9 +1127,6 @@ Side make_side(bool backward, uint32_t* vis, int second) {
 }  // namespace
 
 int ensure_max_degrees(psc_graph_s* g) { return max_degrees_once(g); }
-int vgc_records(psc_graph_s* g, bool backward, const VRec** out) {
-  return ensure_records(g, backward, out);
-}
 
 // Runs the searches of `ns` sides (1 or 2) to completion.  Side k starts from
 // srcs[k], or, when d_srcs is given, every side starts from the n_dsrc device

@@ -1036,16 +1036,9 @@ __global__ void k_build_records(const uint64_t* __restrict__ off, const uint32_t
   }
 }
 
-#ifndef PSC_VGC_RECORDS
-#define PSC_VGC_RECORDS 1
-#endif
 // Once per handle and direction (the graph does not change): the records of
 // the out-lists (backward = false) or in-lists; a symmetric graph shares one.
 static int ensure_records(psc_graph_s* g, bool backward, const VRec** out) {
-  if (!PSC_VGC_RECORDS) {
-    *out = nullptr;
-    return PSC_OK;
-  }
   const int d = (backward && !g->symmetric) ? 1 : 0;
   const int slot = d ? B_REC_B : B_REC_F;
   VRec* r;

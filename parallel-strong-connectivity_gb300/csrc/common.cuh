@@ -115,7 +115,6 @@ struct psc_graph_s {
   int ldd_vgc_blocks = 0; // same for the LDD VGC kernel
   int le_heavy_blocks = 0; // same for the LE-list heavy-pair kernel
   bool deg_known = false;    // max_deg holds the largest out- / in-degree
-  bool rec_ready[2] = {false, false};  // B_REC_F / B_REC_B hold the records
   // per LDD round of the last psc_ldd / psc_cc call: first candidate index,
   // candidates offered, new centres (psc_ldd_rounds)
   std::vector<uint32_t> ldd_trace;
@@ -184,23 +183,8 @@ enum Buf : int {
   B_FLAB,         // u32 labels of a batch's pivots
   B_SCHED,        // window schedule of a batch's prefix-doubling rounds
   B_SCANBITS,     // u32[n/32] selection bits of scan_emit_flags
-  B_REC_F,        // VRec[n] adjacency records of the out-lists (VGC)
-  B_REC_B,        // VRec[n] adjacency records of the in-lists (VGC)
   B_COUNT
 };
-
-// A vertex's adjacency range with its first kRecEdges targets inline, one
-// 32-byte sector: a local search that claims the vertex loads this record
-// alongside the claim, and the next wave reads the targets from it (a cached
-// sector) instead of making another round trip to E.  Unused targets hold
-// UINT32_MAX; deg is capped at UINT32_MAX.
-constexpr int kRecEdges = 5;
-struct __align__(32) VRec {
-  uint64_t beg;
-  uint32_t deg;
-  uint32_t e[kRecEdges];
-};
-static_assert(sizeof(VRec) == 32, "one sector per record");
 
 // Status plumbing: PSC_TRY returns the status of a failing expression.
 #define PSC_TRY(expr)                 \

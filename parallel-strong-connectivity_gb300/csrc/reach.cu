@@ -61,8 +61,6 @@ struct ReachSide {
   // chained VGC rounds: when set, the frontier size is read here (the
   // previous round's ctr->next) instead of nin
   const unsigned long long* nin_dev;
-  // VGC rounds: adjacency records of this direction (null: read off / E)
-  const VRec* rec;
 };
 
 // Lists a vertex with more than kHeavyDeg out-edges for k_reach_heavy.  Its
@@ -261,22 +259,13 @@ __device__ __forceinline__ void vgc_place(uint32_t tm, const uint32_t* w, const 
 // enters the queue with its range and the next wave needs no dependent load.
 template <int K>
 __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, uint64_t* ve,
-                                              const uint64_t* __restrict__ off,
-                                              const VRec* __restrict__ rec, uint32_t* vis) {
+                                              const uint64_t* __restrict__ off, uint32_t* vis) {
 #pragma unroll
   for (int k = 0; k < K; k++) {
     vb[k] = ve[k] = 0;
     if (w[k] != 0xFFFFFFFFu) {
-      if (rec) {
-        // the record's first 16 bytes bring its whole sector (the inline
-        // targets the next wave reads) into the cache
-        const uint4 h = __ldg(reinterpret_cast<const uint4*>(rec + w[k]));
-        vb[k] = (uint64_t)h.x | ((uint64_t)h.y << 32);
-        ve[k] = vb[k] + h.z;
-      } else {
-        vb[k] = __ldg(&off[w[k]]);
-        ve[k] = __ldg(&off[w[k] + 1]);
-      }
+      vb[k] = __ldg(&off[w[k]]);
+      ve[k] = __ldg(&off[w[k] + 1]);
     }
   }
   uint32_t tm = 0;
@@ -330,7 +319,6 @@ __global__ void __launch_bounds__(BLOCK)
     k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau, uint32_t chunk) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ QEnt sq[BLOCK / 32][QCAP];
-  __shared__ uint32_t sv[BLOCK / 32][32];  // the wave's vertices (their records)
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
@@ -421,7 +409,6 @@ __global__ void __launch_bounds__(BLOCK)
       const uint32_t total = __shfl_sync(kFull, incl, 31);
       sm[wid].excl[lane] = incl - deg;
       sm[wid].beg[lane] = beg;
-      sv[wid][lane] = x;
       __syncwarp();
       for (uint32_t base = 0; base < total; base += 32 * K) {
         uint32_t w[K];
@@ -432,12 +419,10 @@ __global__ void __launch_bounds__(BLOCK)
           w[k] = 0xFFFFFFFFu;
           if (gi < total) {
             const int src = find_src(sm[wid], gi);
-            const uint32_t j = gi - sm[wid].excl[src];
-            w[k] = S.rec && j < (uint32_t)kRecEdges ? __ldg(&S.rec[sv[wid][src]].e[j])
-                                                     : __ldg(&S.E[sm[wid].beg[src] + j]);
+            w[k] = __ldg(&S.E[sm[wid].beg[src] + (gi - sm[wid].excl[src])]);
           }
         }
-        const uint32_t tm = vgc_claim<K>(w, vb, ve, S.off, S.rec, S.vis);
+        const uint32_t tm = vgc_claim<K>(w, vb, ve, S.off, S.vis);
         vgc_place<K>(tm, w, vb, ve, Q, tail, tq, S.qout, &S.ctr->next, nedges);
       }
     }
@@ -1018,43 +1003,6 @@ __global__ void k_max_degrees(const uint64_t* __restrict__ off, const uint64_t* 
   }
 }
 
-// Adjacency records (VRec) of one direction: range and first kRecEdges
-// targets of every vertex; one 32-byte record per thread, written as two
-// 16-byte stores.
-__global__ void k_build_records(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
-                                uint64_t n, VRec* rec) {
-  for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t b = off[v], d = off[v + 1] - b;
-    uint32_t e[kRecEdges];
-#pragma unroll
-    for (int j = 0; j < kRecEdges; j++) e[j] = (uint64_t)j < d ? __ldg(&E[b + j]) : 0xFFFFFFFFu;
-    uint4* o = reinterpret_cast<uint4*>(rec + v);
-    o[0] = make_uint4((uint32_t)b, (uint32_t)(b >> 32),
-                      (uint32_t)(d < 0xFFFFFFFFull ? d : 0xFFFFFFFFull), e[0]);
-    o[1] = make_uint4(e[1], e[2], e[3], e[4]);
-  }
-}
-
-// Once per handle and direction (the graph does not change): the records of
-// the out-lists (backward = false) or in-lists; a symmetric graph shares one.
-static int ensure_records(psc_graph_s* g, bool backward, const VRec** out) {
-  const int d = (backward && !g->symmetric) ? 1 : 0;
-  const int slot = d ? B_REC_B : B_REC_F;
-  VRec* r;
-  PSC_TRY(ensure_t(g, slot, g->n + 1, &r));
-  if (!g->rec_ready[d]) {
-    ProfScope ps(g, F_REACH_VGC);
-    ps.bytes = (16.0 + 4.0 * kRecEdges + 32.0) * g->n;
-    k_build_records<<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(d ? g->in_off : g->off,
-                                                                   d ? g->in_E : g->E, g->n, r);
-    PSC_CUDA(cudaGetLastError());
-    g->rec_ready[d] = true;
-  }
-  *out = r;
-  return PSC_OK;
-}
-
 // Once per handle (the graph does not change): max_deg for the heavy-vertex
 // check of chained rounds.
 int max_degrees_once(psc_graph_s* g) {
@@ -1100,7 +1048,6 @@ ReachSide side_args(psc_graph_s* g, const Side& s) {
   r.heavy = (uint64_t*)g->bufs[s.slot_heavy].p;
   r.ctr = g->ctr + s.cset;
   r.nin_dev = nullptr;
-  r.rec = nullptr;
   return r;
 }
 
@@ -1192,7 +1139,6 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           for (int a = 0; a < na; a++) {
             const Side& s = sides[act[a]];
             ReachSide r = side_args(g, s);
-            PSC_TRY(ensure_records(g, s.backward, &r.rec));
             uint32_t* qa = (uint32_t*)g->bufs[s.slot_qa].p;
             uint32_t* qb = (uint32_t*)g->bufs[s.slot_qb].p;
             r.qin = (j & 1) ? qb : qa;
@@ -1278,9 +1224,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
     uint64_t v_items = 0, p_items = 0;
     for (int k = 0; k < ns; k++) {
       if (mode[k] == M_VGC) {
-        vg[nv] = side_args(g, sides[k]);
-        PSC_TRY(ensure_records(g, sides[k].backward, &vg[nv].rec));
-        nv++;
+        vg[nv++] = side_args(g, sides[k]);
         v_items += sides[k].nf;
       } else if (mode[k] == M_PUSH) {
         pu[np++] = side_args(g, sides[k]);

@@ -61,9 +61,9 @@ struct Request {
 // Device bytes a request may need while its batch runs: graph arrays (and for
 // SCC the transpose, plus its build scratch when it is not sent along),
 // labels and the solver's scratch (pivot order, queues, bitmaps, label
-// tables, the local searches' adjacency records) per vertex.
+// tables) per vertex.
 uint64_t request_bytes(int kind, uint64_t n, uint64_t m, bool with_t) {
-  if (kind == PSC_REQ_SCC) return 16 * (n + 1) + (with_t ? 8 : 22) * m + 232 * n;
+  if (kind == PSC_REQ_SCC) return 16 * (n + 1) + (with_t ? 8 : 22) * m + 168 * n;
   return 8 * (n + 1) + 4 * m + 64 * n;
 }
 

@@ -740,66 +740,66 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
-// Pull round with staged tiles: a block's tiles of TV = 32 W (BLOCK / 32)
-// consecutive vertices are taken in grid-stride order; the visited words and
-// the in-list offsets of the tile after next are copied into one of two
-// shared-memory buffers while the current one is worked on, so the loads
-// left on a warp's dependent chain are the first in-edge and the frontier
-// bit.  A tile is staged when its copy stays inside the arrays (offsets
-// [v0, v0 + TV + 2) with v0 + TV + 1 <= n); the last tiles are read from
+// Pull round with staged steps: each warp works through its steps of W words
+// (32 W vertices) in grid-stride order and keeps its own two shared-memory
+// buffers; lane 0 copies the visited words and in-list offsets of the step
+// after next into the buffer just worked on (bulk asynchronous copies on the
+// warp's own mbarrier), so the loads left on the warp's dependent chain are
+// the first in-edge and the frontier bit, and no warp waits for another.  A
+// step is staged when its copy stays inside the arrays (offsets
+// [v0, v0 + 32 W + 2) with v0 + 32 W + 1 <= n); the last steps are read from
 // global memory like k_reach_pull.  A copy that does not arrive within the
-// bounded wait sets ctr->aux1 and the block stops (the host reports it).
+// bounded wait sets ctr->aux1 and the warp stops (the host reports it).
 template <int BLOCK, int W>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     k_reach_pull_staged(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
                         const uint32_t* __restrict__ fb_in, uint32_t* vis, uint32_t* fb_out,
                         uint64_t n, Counters* ctr) {
   constexpr uint32_t NW = BLOCK / 32;
-  constexpr uint32_t TV = NW * 32 * W;  // vertices per tile
-  constexpr uint32_t TW = TV / 32;      // visited words per tile
-  constexpr uint32_t OFF_BYTES = (TV + 2) * 8;
-  constexpr uint32_t VIS_BYTES = TW * 4;
+  constexpr uint32_t SV = 32 * W;  // vertices per step
+  constexpr uint32_t OFF_BYTES = (SV + 2) * 8;
+  constexpr uint32_t VIS_BYTES = W * 4;
   static_assert(OFF_BYTES % 16 == 0 && VIS_BYTES % 16 == 0, "bulk copies of 16-byte multiples");
-  __shared__ __align__(128) uint64_t soff[2][TV + 2];
-  __shared__ __align__(128) uint32_t svis[2][TW];
-  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ __align__(128) uint64_t soff[NW][2][SV + 2];
+  __shared__ __align__(16) uint32_t svis[NW][2][W];
+  __shared__ __align__(8) uint64_t bar[NW][2];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t nwords = (n + 31) >> 5;
-  const uint64_t ntiles = (n + TV - 1) / TV;
-  auto staged = [&](uint64_t tile) { return tile * TV + TV + 1 <= n; };
-  auto issue = [&](uint64_t tile, int buf) {  // one thread
-    mbar_expect_tx(&bar[buf], OFF_BYTES + VIS_BYTES);
-    bulk_copy_g2s(soff[buf], B_off + tile * TV, OFF_BYTES, &bar[buf]);
-    bulk_copy_g2s(svis[buf], vis + tile * TW, VIS_BYTES, &bar[buf]);
+  const uint64_t nsteps = (nwords + W - 1) / W;
+  const uint64_t s0 = (uint64_t)blockIdx.x * NW + wid, sstep = (uint64_t)gridDim.x * NW;
+  auto staged = [&](uint64_t st) { return st * SV + SV + 1 <= n; };
+  auto issue = [&](uint64_t st, int b) {  // lane 0
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar[wid][b], OFF_BYTES + VIS_BYTES);
+    bulk_copy_g2s(soff[wid][b], B_off + st * SV, OFF_BYTES, &bar[wid][b]);
+    bulk_copy_g2s(svis[wid][b], vis + st * W, VIS_BYTES, &bar[wid][b]);
   };
-  if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+  if (lane == 0) {
+    mbar_init(&bar[wid][0], 1);
+    mbar_init(&bar[wid][1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  __syncthreads();
+  __syncwarp();
   // bit b: the phase parity to wait for / a copy in flight, of buffer b
   uint32_t parity = 0, pending = 0;
-  const uint64_t t0 = blockIdx.x, tstep = gridDim.x;
-  for (int bb = 0; bb < 2; bb++) {
-    const uint64_t tile = t0 + bb * tstep;
-    if (tile < ntiles && staged(tile)) {
-      if (threadIdx.x == 0) issue(tile, bb);
-      pending |= 1u << bb;
+  for (int b = 0; b < 2; b++) {
+    const uint64_t st = s0 + b * sstep;
+    if (st < nsteps && staged(st)) {
+      if (lane == 0) issue(st, b);
+      pending |= 1u << b;
     }
   }
   unsigned long long cnt = 0, scanned = 0, unvisited = 0;
   bool failed = false;
   int buf = 0;
-  for (uint64_t tile = t0; tile < ntiles; tile += tstep, buf ^= 1) {
-    const uint64_t w = tile * TW + wid * W;  // this warp's first word
+  for (uint64_t st = s0; st < nsteps; st += sstep, buf ^= 1) {
+    const uint64_t w = st * W;
     uint32_t vw[W];
     bool t[W];
     uint64_t b[W], e[W];
     if ((pending >> buf) & 1u) {
-      // every thread waits for the tile; giving up is decided block-wide
-      const bool ok = mbar_wait_bounded(&bar[buf], (parity >> buf) & 1u);
-      if (__syncthreads_or(!ok)) {
+      const bool ok = mbar_wait_bounded(&bar[wid][buf], (parity >> buf) & 1u);
+      if (__any_sync(kFull, !ok)) {  // giving up is decided warp-wide
         failed = true;
         break;
       }
@@ -807,36 +807,32 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
       pending &= ~(1u << buf);
 #pragma unroll
       for (int k = 0; k < W; k++) {
-        const uint32_t li = (wid * W + k) * 32 + lane;
-        vw[k] = svis[buf][wid * W + k];
+        const uint32_t li = k * 32 + lane;
+        vw[k] = svis[wid][buf][k];
         t[k] = !((vw[k] >> lane) & 1u);
         b[k] = e[k] = 0;
         if (t[k]) {
-          b[k] = soff[buf][li];
-          e[k] = soff[buf][li + 1];
+          b[k] = soff[wid][buf][li];
+          e[k] = soff[wid][buf][li + 1];
         }
         unvisited += t[k] ? 1 : 0;
+      }
+      // every lane has its values: the buffer may take the step after next
+      __syncwarp();
+      const uint64_t nt = st + 2 * sstep;
+      if (nt < nsteps && staged(nt)) {
+        if (lane == 0) issue(nt, buf);
+        pending |= 1u << buf;
       }
     } else {
       pull_load_global<W>(w, nwords, n, B_off, vis, vw, t, b, e, unvisited);
     }
     pull_step<W>(w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
-    // every warp is done with this buffer before the copy of the tile after
-    // next lands in it
-    __syncthreads();
-    const uint64_t nt = tile + 2 * tstep;
-    if (nt < ntiles && staged(nt)) {
-      if (threadIdx.x == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue(nt, buf);
-      }
-      pending |= 1u << buf;
-    }
   }
   if (failed) {
     // the copies still in flight land before the block's shared memory goes
-    if (pending & 1u) mbar_wait_bounded(&bar[0], parity & 1u);
-    if (pending & 2u) mbar_wait_bounded(&bar[1], (parity >> 1) & 1u);
+    if (pending & 1u) mbar_wait_bounded(&bar[wid][0], parity & 1u);
+    if (pending & 2u) mbar_wait_bounded(&bar[wid][1], (parity >> 1) & 1u);
     if (lane == 0) atomicOr(&ctr->aux1, 1ull);
   }
   flush_pull_counters(ctr, cnt, scanned, unvisited);
@@ -865,7 +861,7 @@ static unsigned pull_grid(int num_sms, uint64_t nwords) {
   return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
 }
 
-constexpr uint64_t kPullStagedTile = (uint64_t)kReachBlock * kPullW;  // vertices of a staged tile
+constexpr uint64_t kPullStagedTile = 32ull * kPullW;  // vertices of a staged warp step
 
 constexpr uint64_t kPullExactBelow = 1u << 14;
 constexpr uint32_t kSampleProbes = 32 * 64;

@@ -167,10 +167,13 @@ int scc_partition(psc_graph_s* g, const MsResult res[2], uint64_t* labels) {
   return PSC_OK;
 }
 
-// Batches of at most this many candidate pivots start asynchronously (see
-// the batch loop below); larger ones wait for their pivot count, which sizes
-// their tables.
-constexpr uint64_t kAsyncBatch = 1u << 16;
+// Batches whose candidate pivots fit the multi-search's VGC range (one pair
+// per resident warp, num_sms * 32) start asynchronously (see the batch loop
+// below): their upper bound chooses the same VGC sub-round as the pivot count
+// would, and sizes their tables modestly.  Larger ones wait for the count.
+#ifndef PSC_ASYNC_BATCHES
+#define PSC_ASYNC_BATCHES 1
+#endif
 
 static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
   const uint64_t n = g->n;
@@ -235,7 +238,7 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
       // Small batches start without waiting for their pivot count: the
       // compaction's total is read on the device by the seeds and the first
       // sub-round, so the batch waits on the host once per sub-round only.
-      const bool async = vs_size <= kAsyncBatch;
+      const bool async = PSC_ASYNC_BATCHES && p->local_scc && vs_size <= (uint64_t)g->num_sms * 32;
       uint64_t nf = 0;
       const unsigned long long* nf_dev = nullptr;
       PSC_TRY(scan_emit_flags(g, vs_size, NotDoneAt{centers, labels, cur_offset},

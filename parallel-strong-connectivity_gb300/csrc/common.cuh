@@ -257,8 +257,10 @@ __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 // Rejects a CSR whose offsets do not run from 0 to m without decreasing or
 // whose targets are not vertex ids: sets *bad.  Only the arrays themselves
 // are read (no access is indexed by their values), so any input of the
-// declared sizes is safe to check.  A template so that every translation
-// unit that launches it holds its own instance.
+// declared sizes is safe to check.  16-byte aligned arrays are read with
+// 128-bit loads (two offsets or four targets per load); others one element
+// at a time.  A template so that every translation unit that launches it
+// holds its own instance.
 template <int kUnused = 0>
 __global__ void k_validate_csr(const uint64_t* __restrict__ off, uint64_t n,
                                const uint32_t* __restrict__ E, uint64_t m,
@@ -266,8 +268,29 @@ __global__ void k_validate_csr(const uint64_t* __restrict__ off, uint64_t n,
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool b = t == 0 && (off[0] != 0 || off[n] != m);
-  for (uint64_t v = t; v < n; v += stride) b |= off[v] > off[v + 1];
-  for (uint64_t i = t; i < m; i += stride) b |= E[i] >= n;
+  if (((uintptr_t)off & 15) == 0) {
+    // pair j = off[2j], off[2j + 1]; its successor off[2j + 2] (<= off[n])
+    const uint64_t np = n / 2;
+    const ulonglong2* o2 = reinterpret_cast<const ulonglong2*>(off);
+    for (uint64_t j = t; j < np; j += stride) {
+      const ulonglong2 a = __ldg(&o2[j]);
+      b |= a.x > a.y || a.y > __ldg(&off[2 * j + 2]);
+    }
+    if ((n & 1) && t == 0) b |= off[n - 1] > off[n];
+  } else {
+    for (uint64_t v = t; v < n; v += stride) b |= off[v] > off[v + 1];
+  }
+  if (((uintptr_t)E & 15) == 0) {
+    const uint64_t nq = m / 4;
+    const uint4* e4 = reinterpret_cast<const uint4*>(E);
+    for (uint64_t q = t; q < nq; q += stride) {
+      const uint4 x = __ldg(&e4[q]);
+      b |= x.x >= n || x.y >= n || x.z >= n || x.w >= n;
+    }
+    for (uint64_t i = nq * 4 + t; i < m; i += stride) b |= E[i] >= n;
+  } else {
+    for (uint64_t i = t; i < m; i += stride) b |= E[i] >= n;
+  }
   if (__any_sync(kFull, b) && lane_id() == 0) atomicOr(bad, 1ull);
 }
 

@@ -23,6 +23,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cstdio>
+
 #include "common.cuh"
 #include "engines.cuh"
 #include "scan.cuh"
@@ -736,6 +738,17 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
     }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(read_counters(g));
+    if (trace_on()) {  // ms since the start of the call (the stream is idle here)
+      cudaEvent_t ev = take_event(g);
+      PSC_CUDA(cudaEventRecord(ev, g->stream));
+      PSC_CUDA(cudaEventSynchronize(ev));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, g->t0, ev);
+      give_event(g, ev);
+      std::fprintf(stderr, "ldd round %u mode %s nf %llu new_centres %u next %llu edges %llu t %.3f ms\n",
+                   round, pull ? "pull" : "push", (unsigned long long)nf, new_centres,
+                   g->hctr[0].next, g->hctr[0].edges, ms);
+    }
     if (g->profiling) {
       // algorithmic bytes: push / VGC: 16 per frontier vertex (range), 8 per
       // edge (target id, label CAS), 8 per new vertex; pull: both bitmaps,
@@ -869,6 +882,15 @@ int cc_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* d_forest, u
   }
   PSC_TRY(uf_bytes(uf_edges1));
   PSC_CUDA(cudaGetLastError());
+  if (trace_on()) {
+    cudaEvent_t ev = take_event(g);
+    PSC_CUDA(cudaEventRecord(ev, g->stream));
+    PSC_CUDA(cudaEventSynchronize(ev));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, g->t0, ev);
+    give_event(g, ev);
+    std::fprintf(stderr, "cc union-find done t %.3f ms\n", ms);
+  }
   if (n_forest) {
     PSC_TRY(read_counters(g));
     *n_forest = g->hctr[0].aux1;

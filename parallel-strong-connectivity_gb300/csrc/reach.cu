@@ -514,11 +514,14 @@ __global__ void __launch_bounds__(BLOCK) k_reach_heavy(ReachSide s0, ReachSide s
   }
 }
 
-// Pull round: B_* is the reverse direction of the search.  A warp owns 32 W
-// consecutive vertices per step; each unvisited one looks through its
-// in-edges for a frontier vertex (pull_step below), kPullP edges per lane in
-// flight.
+// Pull round: B_* is the reverse direction of the search, A_off the search
+// direction's offsets (for the next round's edge count).  A warp owns 32
+// consecutive vertices; each unvisited one scans its in-edges for a frontier
+// vertex, kPullP edges in flight, alone for its first kPullSolo in-edges; the
+// longer in-lists left over are then scanned by the whole warp, one vertex at
+// a time, 32 * kPullP edges per step, until a hit.
 constexpr int kPullP = 4;
+constexpr uint32_t kPullSolo = 64;
 #ifndef PSC_PULL_W
 #define PSC_PULL_W 4
 #endif
@@ -532,8 +535,33 @@ __device__ __forceinline__ bool fb_test(const uint32_t* __restrict__ fb, uint32_
   return (__ldg(&fb[x >> 5]) >> (x & 31)) & 1u;
 }
 
-// The whole warp scans the in-lists too long for pull_balanced, one vertex
-// at a time, 32 * kPullP in-edges per step, until a hit.
+// Solo scan of one unvisited vertex's in-list [j, lim): kPullP in-edges at a
+// time until a frontier in-neighbour is found.
+__device__ __forceinline__ bool pull_scan(const uint32_t* __restrict__ B_E,
+                                          const uint32_t* __restrict__ fb_in, uint64_t& j,
+                                          uint64_t lim) {
+  bool found = false;
+  while (j < lim && !found) {
+    uint32_t x[kPullP];
+#pragma unroll
+    for (int k = 0; k < kPullP; k++) x[k] = j + k < lim ? __ldg(&B_E[j + k]) : 0xFFFFFFFFu;
+    bool hit[kPullP];
+#pragma unroll
+    for (int k = 0; k < kPullP; k++) hit[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
+    uint64_t step = lim - j < (uint64_t)kPullP ? lim - j : (uint64_t)kPullP;
+#pragma unroll
+    for (int k = kPullP - 1; k >= 0; k--)
+      if (hit[k]) {
+        found = true;
+        step = k + 1;
+      }
+    j += step;
+  }
+  return found;
+}
+
+// The whole warp scans the in-lists left over from the solo phase, one
+// vertex at a time, 32 * kPullP in-edges per step, until a hit.
 __device__ __forceinline__ void pull_long(const uint32_t* __restrict__ B_E,
                                           const uint32_t* __restrict__ fb_in, uint32_t longm,
                                           uint64_t j, uint64_t e, bool& found,
@@ -559,98 +587,44 @@ __device__ __forceinline__ void pull_long(const uint32_t* __restrict__ B_E,
   }
 }
 
-// Warp-wide scan of the lanes' remaining in-lists [j, e) (one per lane,
-// empty unless `active`): their concatenation is walked 32 * kPullP edges per
-// step, each lane testing one edge of some list, so the walk takes
-// (sum of lengths) / (32 * kPullP) dependent steps instead of the longest
-// list's length; a list is no longer read once one of its edges hit, and the
-// walk stops when every list has a hit or is done.  Consecutive vertices'
-// in-lists are adjacent in B_E, so the loads of a step are coalesced.
-__device__ __forceinline__ void pull_balanced(WarpExpandSmem& sm, const uint32_t* __restrict__ B_E,
-                                              const uint32_t* __restrict__ fb_in, bool active,
-                                              bool& f, uint64_t j, uint64_t e,
-                                              unsigned long long& scanned) {
-  const unsigned lane = lane_id();
-  const uint32_t len = active ? (uint32_t)(e - j) : 0u;
-  uint32_t incl = len;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(kFull, incl, o);
-    if ((int)lane >= o) incl += t;
-  }
-  const uint32_t total = __shfl_sync(kFull, incl, 31);
-  if (total == 0) return;  // warp-uniform
-  sm.excl[lane] = incl - len;
-  sm.beg[lane] = j;
-  __syncwarp();
-  const uint32_t need = __ballot_sync(kFull, len > 0);
-  uint32_t got = 0;
-  for (uint32_t base = 0; base < total && (need & ~got); base += 32 * kPullP) {
-    uint32_t x[kPullP];
-    int src[kPullP];
-#pragma unroll
-    for (int p = 0; p < kPullP; p++) {
-      const uint32_t gi = base + p * 32 + lane;
-      x[p] = 0xFFFFFFFFu;
-      src[p] = 0;
-      if (gi < total) {
-        src[p] = find_src(sm, gi);
-        if (!((got >> src[p]) & 1u)) {
-          x[p] = __ldg(&B_E[sm.beg[src[p]] + (gi - sm.excl[src[p]])]);
-          scanned++;
-        }
-      }
-    }
-    uint32_t hits = 0;
-#pragma unroll
-    for (int p = 0; p < kPullP; p++)
-      if (x[p] != 0xFFFFFFFFu && fb_test(fb_in, x[p])) hits |= 1u << src[p];
-    got |= __reduce_or_sync(kFull, hits);
-  }
-  f = f || ((got >> lane) & 1u);
-  __syncwarp();
-}
-
 // One warp step of a pull round over W adjacent bitmap words (32 W vertices)
 // starting at word w: lane's vertex of word k is unvisited when t[k], with
 // in-list [b[k], e[k]).  The first in-edges of all W vertices are loaded
-// together (dense rounds often hit at once); then, word by word, the whole
-// warp walks the remaining in-lists of up to kPullBal edges
-// (pull_balanced), and longer ones one vertex at a time (pull_long); the
-// words' new frontier bits are written with one store each.
-constexpr uint64_t kPullBal = 256;
-
+// together (dense rounds often hit at once), then each unvisited vertex
+// scans alone, then the long in-lists left over are scanned by the whole
+// warp; the words' new frontier bits are written with one store each.
 template <int W>
-__device__ __forceinline__ void pull_step(WarpExpandSmem& sm, uint64_t w, uint64_t nwords,
-                                          const uint32_t* vw, const bool* t, const uint64_t* b,
-                                          const uint64_t* e, const uint32_t* __restrict__ B_E,
+__device__ __forceinline__ void pull_step(uint64_t w, uint64_t nwords, const uint32_t* vw,
+                                          const bool* t, const uint64_t* b, const uint64_t* e,
+                                          const uint32_t* __restrict__ B_E,
                                           const uint32_t* __restrict__ fb_in, uint32_t* vis,
                                           uint32_t* fb_out, unsigned long long& cnt,
                                           unsigned long long& scanned) {
   const unsigned lane = lane_id();
   bool f[W];
-  uint64_t j[W];
+  uint64_t j[W], lim[W];
   uint32_t x[W];
 #pragma unroll
   for (int k = 0; k < W; k++) {
+    lim[k] = e[k] < b[k] + kPullSolo ? e[k] : b[k] + kPullSolo;
     j[k] = b[k];
-    x[k] = t[k] && j[k] < e[k] ? __ldg(&B_E[j[k]]) : 0xFFFFFFFFu;
+    x[k] = t[k] && j[k] < lim[k] ? __ldg(&B_E[j[k]]) : 0xFFFFFFFFu;
   }
 #pragma unroll
   for (int k = 0; k < W; k++) {
     f[k] = x[k] != 0xFFFFFFFFu && fb_test(fb_in, x[k]);
-    if (t[k] && j[k] < e[k]) {
-      j[k]++;
-      scanned++;
-    }
+    if (t[k] && j[k] < lim[k]) j[k]++;
   }
 #pragma unroll
-  for (int k = 0; k < W; k++) {
-    const bool rest = t[k] && !f[k] && j[k] < e[k];
-    pull_balanced(sm, B_E, fb_in, rest && e[k] - j[k] <= kPullBal, f[k], j[k], e[k], scanned);
-    pull_long(B_E, fb_in, __ballot_sync(kFull, rest && e[k] - j[k] > kPullBal), j[k], e[k], f[k],
+  for (int k = 0; k < W; k++)
+    if (t[k] && !f[k]) f[k] = pull_scan(B_E, fb_in, j[k], lim[k]);
+#pragma unroll
+  for (int k = 0; k < W; k++)
+    if (t[k]) scanned += j[k] - b[k];
+#pragma unroll
+  for (int k = 0; k < W; k++)
+    pull_long(B_E, fb_in, __ballot_sync(kFull, t[k] && !f[k] && j[k] < e[k]), j[k], e[k], f[k],
               scanned);
-  }
 #pragma unroll
   for (int k = 0; k < W; k++) {
     const uint32_t mk = __ballot_sync(kFull, f[k]);
@@ -706,7 +680,6 @@ __global__ void __launch_bounds__(BLOCK)
     k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
                  const uint32_t* __restrict__ fb_in, uint32_t* vis, uint32_t* fb_out, uint64_t n,
                  Counters* ctr) {
-  __shared__ WarpExpandSmem sm[BLOCK / 32];
   const unsigned wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
@@ -717,7 +690,7 @@ __global__ void __launch_bounds__(BLOCK)
     bool t[W];
     uint64_t b[W], e[W];
     pull_load_global<W>(w, nwords, n, B_off, vis, vw, t, b, e, unvisited);
-    pull_step<W>(sm[wid], w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
+    pull_step<W>(w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
   }
   flush_pull_counters(ctr, cnt, scanned, unvisited);
 }
@@ -790,7 +763,6 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
   __shared__ __align__(128) uint64_t soff[NW][2][SV + 2];
   __shared__ __align__(16) uint32_t svis[NW][2][W];
   __shared__ __align__(8) uint64_t bar[NW][2];
-  __shared__ WarpExpandSmem sm[NW];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t nwords = (n + 31) >> 5;
   const uint64_t nsteps = (nwords + W - 1) / W;
@@ -855,7 +827,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
     } else {
       pull_load_global<W>(w, nwords, n, B_off, vis, vw, t, b, e, unvisited);
     }
-    pull_step<W>(sm[wid], w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
+    pull_step<W>(w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
   }
   if (failed) {
     // the copies still in flight land before the block's shared memory goes

@@ -229,6 +229,18 @@ struct QEnt {
 // Spills of a VGC warp: `total` vertices, the first ndq into the donation
 // queue (slots dq_base ...), the rest into the next frontier (q_base ...).
 // One reservation (lane 0) for the warp, broadcast to all lanes.
+// Donation slots are written and polled with relaxed GPU-scope accesses in
+// volatile asm: a poll is never hoisted out of its loop, and never served from
+// a stale L1 line.
+__device__ __forceinline__ unsigned long long slot_load(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void slot_store(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 struct SpillBase {
   unsigned long long dq_base, q_base;
   uint32_t ndq, tag;
@@ -260,7 +272,7 @@ __device__ __forceinline__ SpillBase spill_reserve(const ReachSide& S, uint32_t 
 __device__ __forceinline__ void spill_put(const ReachSide& S, const SpillBase& sb, uint32_t i,
                                           uint32_t v, uint64_t deg, unsigned long long& nedges) {
   if (i < sb.ndq) {
-    __stcg(&S.dq[sb.dq_base + i], ((unsigned long long)sb.tag << 32) | v);
+    slot_store(&S.dq[sb.dq_base + i], ((unsigned long long)sb.tag << 32) | v);
   } else {
     S.qout[sb.q_base + (i - sb.ndq)] = v;
     nedges += deg;
@@ -300,12 +312,18 @@ __device__ __forceinline__ void vgc_place(uint32_t tm, const uint32_t* w, const 
   __syncwarp();
 }
 
-// Claims of one batch: each candidate's adjacency range is loaded alongside
-// its claim (speculatively: wasted when the claim fails), so a claimed vertex
-// enters the queue with its range and the next wave needs no dependent load.
+// Claims of one batch: a claimed vertex enters the queue with its adjacency
+// range, so the next wave needs no dependent load.  With PSC_VGC_SPEC the
+// range is loaded alongside the claim (speculatively: wasted traffic when the
+// claim fails, but off the claim's latency chain); without it, only after a
+// claim succeeds.
+#ifndef PSC_VGC_SPEC
+#define PSC_VGC_SPEC 1
+#endif
 template <int K>
 __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, uint64_t* ve,
                                               const uint64_t* __restrict__ off, uint32_t* vis) {
+#if PSC_VGC_SPEC
 #pragma unroll
   for (int k = 0; k < K; k++) {
     vb[k] = ve[k] = 0;
@@ -314,6 +332,7 @@ __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, u
       ve[k] = __ldg(&off[w[k] + 1]);
     }
   }
+#endif
   uint32_t tm = 0;
 #pragma unroll
   for (int k = 0; k < K; k++)
@@ -321,6 +340,16 @@ __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, u
       const uint32_t b = 1u << (w[k] & 31);
       if (!(atomicOr(&vis[w[k] >> 5], b) & b)) tm |= 1u << k;
     }
+#if !PSC_VGC_SPEC
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    vb[k] = ve[k] = 0;
+    if (tm & (1u << k)) {
+      vb[k] = __ldg(&off[w[k]]);
+      ve[k] = __ldg(&off[w[k] + 1]);
+    }
+  }
+#endif
   return tm;
 }
 
@@ -513,8 +542,8 @@ __global__ void __launch_bounds__(BLOCK, K <= 4 ? 6 : 5)
           const ReachSide& S = side ? s1 : s0;
           if (!S.dq) continue;
           for (int attempt = 0; attempt < 64; attempt++) {
-            const unsigned long long hh = *(volatile unsigned long long*)&S.ctr->pad[0];
-            unsigned long long tt = *(volatile unsigned long long*)&S.ctr->pad[1];
+            const unsigned long long hh = slot_load(&S.ctr->pad[0]);
+            unsigned long long tt = slot_load(&S.ctr->pad[1]);
             if (tt > kDonCap) tt = kDonCap;
             if (hh >= tt) break;
             const unsigned long long nh = hh + C < tt ? hh + C : tt;
@@ -536,8 +565,9 @@ __global__ void __launch_bounds__(BLOCK, K <= 4 ? 6 : 5)
       bool ok = true;
       if (lane < cnt) {
         const unsigned long long* slot = &S.dq[h + lane];
-        unsigned long long e = __ldcv(slot);
-        for (uint32_t spin = 0; (uint32_t)(e >> 32) != tag && spin < kDonSpin; spin++) e = __ldcv(slot);
+        unsigned long long e = slot_load(slot);
+        for (uint32_t spin = 0; (uint32_t)(e >> 32) != tag && spin < kDonSpin; spin++)
+          e = slot_load(slot);
         ok = (uint32_t)(e >> 32) == tag;
         u = (uint32_t)e;
       }
@@ -570,17 +600,17 @@ __global__ void __launch_bounds__(BLOCK, K <= 4 ? 6 : 5)
         const ReachSide& S = sd ? s1 : s0;
         if (!S.dq) continue;
         unsigned long long& nedges = sd ? nedges1 : nedges0;
-        const unsigned long long hh = *(volatile unsigned long long*)&S.ctr->pad[0];
-        unsigned long long tt = *(volatile unsigned long long*)&S.ctr->pad[1];
+        const unsigned long long hh = slot_load(&S.ctr->pad[0]);
+        unsigned long long tt = slot_load(&S.ctr->pad[1]);
         if (tt > kDonCap) tt = kDonCap;
         for (unsigned long long b = hh; b < tt; b += 32) {
           const unsigned long long i = b + lane;
           bool take = false;
           uint32_t v = 0;
           if (i < tt) {
-            unsigned long long e = __ldcv(&S.dq[i]);
+            unsigned long long e = slot_load(&S.dq[i]);
             for (uint32_t spin = 0; (uint32_t)(e >> 32) != tag && spin < kDonSpin; spin++)
-              e = __ldcv(&S.dq[i]);
+              e = slot_load(&S.dq[i]);
             take = (uint32_t)(e >> 32) == tag;
             if (!take) atomicOr(&s0.ctr->aux0, 1ull);
             v = (uint32_t)e;

@@ -111,7 +111,6 @@ struct psc_graph_s {
   uint32_t* in_E = nullptr;
   int num_sms = 0;
   int vgc_blocks = 0;     // resident blocks per SM of the reach VGC kernel
-  uint32_t vgc_tag = 0;   // launch tag of the VGC rounds' donation queues
   int ms_vgc_blocks = 0;  // same for the multi-search VGC kernel
   int ldd_vgc_blocks = 0; // same for the LDD VGC kernel
   int le_heavy_blocks = 0; // same for the LE-list heavy-pair kernel
@@ -184,7 +183,6 @@ enum Buf : int {
   B_FLAB,         // u32 labels of a batch's pivots
   B_SCHED,        // window schedule of a batch's prefix-doubling rounds
   B_SCANBITS,     // u32[n/32] selection bits of scan_emit_flags
-  B_DQ,           // u64 donation queues of the VGC rounds (two sides)
   B_COUNT
 };
 

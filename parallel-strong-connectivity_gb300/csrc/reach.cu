@@ -61,16 +61,7 @@ struct ReachSide {
   // chained VGC rounds: when set, the frontier size is read here (the
   // previous round's ctr->next) instead of nin
   const unsigned long long* nin_dev;
-  // VGC rounds: the side's donation queue (null: spills go to qout only);
-  // its head and tail are ctr->pad[0] and ctr->pad[1]
-  unsigned long long* dq;
 };
-
-// Donation queue of a VGC round (k_reach_vgc): kDonCap slots of
-// tag << 32 | vertex, where tag identifies the launch, so a slot written by
-// an earlier launch is never taken for one of this launch's.
-constexpr uint32_t kDonCap = 1u << 16;
-constexpr uint32_t kDonSpin = 1u << 20;  // polls of a reserved slot before giving up
 
 // Lists a vertex with more than kHeavyDeg out-edges for k_reach_heavy.  Its
 // edges are cut into chunks of kHeavyChunk; one 64-bit atomic on ctr->heavy =
@@ -226,63 +217,10 @@ struct QEnt {
 // Places this lane's claimed candidates (bit k of tm <=> w[k] claimed) into the
 // warp's local queue while it has room, then spills the rest to the global
 // frontier: one warp scan and at most one global atomic for the whole warp.
-// Spills of a VGC warp: `total` vertices, the first ndq into the donation
-// queue (slots dq_base ...), the rest into the next frontier (q_base ...).
-// One reservation (lane 0) for the warp, broadcast to all lanes.
-// Donation slots are written and polled with relaxed GPU-scope accesses in
-// volatile asm: a poll is never hoisted out of its loop, and never served from
-// a stale L1 line.
-__device__ __forceinline__ unsigned long long slot_load(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void slot_store(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-struct SpillBase {
-  unsigned long long dq_base, q_base;
-  uint32_t ndq, tag;
-};
-
-__device__ __forceinline__ SpillBase spill_reserve(const ReachSide& S, uint32_t total,
-                                                   uint32_t tag) {
-  SpillBase sb{0, 0, 0, tag};
-  if (total == 0) return sb;
-  if (lane_id() == 0) {
-    uint32_t ndq = 0;
-    if (S.dq) {
-      const unsigned long long r = atomicAdd(&S.ctr->pad[1], (unsigned long long)total);
-      if (r < kDonCap) {
-        ndq = kDonCap - r < total ? (uint32_t)(kDonCap - r) : total;
-        sb.dq_base = r;
-      }
-    }
-    sb.ndq = ndq;
-    if (total > ndq) sb.q_base = atomicAdd(&S.ctr->next, (unsigned long long)(total - ndq));
-  }
-  sb.dq_base = __shfl_sync(kFull, sb.dq_base, 0);
-  sb.q_base = __shfl_sync(kFull, sb.q_base, 0);
-  sb.ndq = __shfl_sync(kFull, sb.ndq, 0);
-  return sb;
-}
-
-// Spill i of a reservation: vertex v with out-degree deg.
-__device__ __forceinline__ void spill_put(const ReachSide& S, const SpillBase& sb, uint32_t i,
-                                          uint32_t v, uint64_t deg, unsigned long long& nedges) {
-  if (i < sb.ndq) {
-    slot_store(&S.dq[sb.dq_base + i], ((unsigned long long)sb.tag << 32) | v);
-  } else {
-    S.qout[sb.q_base + (i - sb.ndq)] = v;
-    nedges += deg;
-  }
-}
-
 template <int K>
 __device__ __forceinline__ void vgc_place(uint32_t tm, const uint32_t* w, const uint64_t* vb,
                                           const uint64_t* ve, QEnt* Q, uint32_t& tail, uint32_t tq,
-                                          const ReachSide& S, uint32_t tag,
+                                          uint32_t* qout, unsigned long long* next_ctr,
                                           unsigned long long& nedges) {
   const unsigned lane = lane_id();
   const uint32_t cnt = __popc(tm);
@@ -296,16 +234,20 @@ __device__ __forceinline__ void vgc_place(uint32_t tm, const uint32_t* w, const 
   if (total == 0) return;
   const uint32_t room = tail < tq ? tq - tail : 0;
   const uint32_t nloc = total < room ? total : room;
-  const SpillBase sb = spill_reserve(S, total - nloc, tag);
+  unsigned long long sbase = 0;
+  if (total > nloc && lane == 0) sbase = atomicAdd(next_ctr, (unsigned long long)(total - nloc));
+  sbase = __shfl_sync(kFull, sbase, 0);
   uint32_t r = incl - cnt;
 #pragma unroll
   for (int k = 0; k < K; k++)
     if (tm & (1u << k)) {
       const uint64_t vd = ve[k] - vb[k];
-      if (r < nloc)
+      if (r < nloc) {
         Q[tail + r] = QEnt{vb[k], w[k], (uint32_t)(vd < 0xFFFFFFFFull ? vd : 0xFFFFFFFFull)};
-      else
-        spill_put(S, sb, r - nloc, w[k], vd, nedges);
+      } else {
+        qout[sbase + (r - nloc)] = w[k];
+        nedges += vd;
+      }
       r++;
     }
   tail += nloc;
@@ -389,20 +331,9 @@ __device__ __forceinline__ void vgc_direct(const ReachSide& S, uint64_t ub, uint
 // out-edges, and whatever is left in the queue when it fills or after
 // max_waves waves, are spilled too.
 // Other chunk vertices are expanded directly (heavy ones by the whole grid).
-//
-// Donation: when the sides carry donation queues, spills go first into them
-// (tagged slots, see kDonCap), and a warp that is done with its chunks of the
-// frontier takes vertices other warps have spilled in this launch and runs
-// local searches from them, instead of idling until the longest search of the
-// round ends.  A warp takes only slots already reserved (CAS on the head, never
-// past the tail) and waits, bounded, for the reserving warp to write them; an
-// empty queue means it exits.  The last warp to exit moves what is left in the
-// queues into the next frontier.  Reachability is unchanged: a vertex is
-// claimed on the visited bitmap once and expanded once, in this launch or in
-// the next round.  A slot that never shows its write sets s0.ctr->aux0.
 template <int BLOCK, int QCAP, int K>
-__global__ void __launch_bounds__(BLOCK, K <= 4 ? 6 : 5)
-    k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau, uint32_t chunk, uint32_t tag) {
+__global__ void __launch_bounds__(BLOCK)
+    k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau, uint32_t chunk) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ QEnt sq[BLOCK / 32][QCAP];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -426,13 +357,18 @@ __global__ void __launch_bounds__(BLOCK, K <= 4 ? 6 : 5)
   QEnt* Q = sq[wid];
   unsigned long long scanned0 = 0, scanned1 = 0, nedges0 = 0, nedges1 = 0, exp0 = 0, exp1 = 0;
   unsigned long long wv0 = 0, wv1 = 0;  // waves (warp-uniform)
-
-  // One chunk of side sd: lanes below cnt hold frontier vertex u.
-  auto run_chunk = [&](int sd, uint32_t cnt, uint32_t u) {
-    const ReachSide& S = sd ? s1 : s0;
+  const uint64_t c0 = (s0.nin + C - 1) / C, c1 = (s1.nin + C - 1) / C;
+  for (uint64_t c = gw; c < c0 + c1; c += nw) {
+    const int sd = c < c0 ? 0 : 1;
+    const ReachSide S = sd ? s1 : s0;
     unsigned long long& nedges = sd ? nedges1 : nedges0;
+    const uint64_t first = (sd ? c - c0 : c) * C;
+    const uint64_t left = S.nin - first;
+    const uint32_t cnt = left < C ? (uint32_t)left : C;
+    uint32_t u = 0;
     uint64_t ub = 0, du = 0;
     if (lane < cnt) {
+      u = S.qin[first + lane];
       ub = S.off[u];
       du = S.off[u + 1] - ub;
       (sd ? exp1 : exp0)++;
@@ -472,10 +408,12 @@ __global__ void __launch_bounds__(BLOCK, K <= 4 ? 6 : 5)
       head += wave;
       (sd ? wv1 : wv0)++;
       __syncwarp();
-      const uint32_t sm_self = __ballot_sync(kFull, spill_self);
-      if (sm_self) {
-        const SpillBase sb = spill_reserve(S, __popc(sm_self), tag);
-        if (spill_self) spill_put(S, sb, __popc(sm_self & ((1u << lane) - 1)), x, xdeg, nedges);
+      if (__any_sync(kFull, spill_self)) {
+        unsigned long long pos = warp_append(&S.ctr->next, spill_self);
+        if (spill_self) {
+          S.qout[pos] = x;
+          nedges += xdeg;
+        }
       }
       (sd ? scanned1 : scanned0) += deg;
       // balanced expansion over the wave's edges, 32*K per batch
@@ -502,127 +440,26 @@ __global__ void __launch_bounds__(BLOCK, K <= 4 ? 6 : 5)
           }
         }
         const uint32_t tm = vgc_claim<K>(w, vb, ve, S.off, S.vis);
-        vgc_place<K>(tm, w, vb, ve, Q, tail, tq, S, tag, nedges);
+        vgc_place<K>(tm, w, vb, ve, Q, tail, tq, S.qout, &S.ctr->next, nedges);
       }
     }
     // spill what is left in the queue with one reservation
     const uint32_t rem = tail - head;
     if (rem) {
-      const SpillBase sb = spill_reserve(S, rem, tag);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&S.ctr->next, (unsigned long long)rem);
+      base = __shfl_sync(kFull, base, 0);
       for (uint32_t k = lane; k < rem; k += 32) {
         const QEnt q = Q[head + k];
-        spill_put(S, sb, k, q.v, q.deg, nedges);
+        S.qout[base + k] = q.v;
+        nedges += q.deg;
       }
     }
     __syncwarp();
-  };
-
-  // the round's frontier, in chunks over the grid
-  const uint64_t c0 = (s0.nin + C - 1) / C, c1 = (s1.nin + C - 1) / C;
-  for (uint64_t c = gw; c < c0 + c1; c += nw) {
-    const int sd = c < c0 ? 0 : 1;
-    const ReachSide& S = sd ? s1 : s0;
-    const uint64_t first = (sd ? c - c0 : c) * C;
-    const uint64_t left = S.nin - first;
-    const uint32_t cnt = left < C ? (uint32_t)left : C;
-    const uint32_t u = lane < cnt ? S.qin[first + lane] : 0u;
-    run_chunk(sd, cnt, u);
   }
-
-  // then vertices other warps spilled in this launch
-  bool lost = false;
-  if (s0.dq) {
-    // each pass takes at least one slot: at most 2 * kDonCap passes
-    for (;;) {
-      int sd = -1;
-      unsigned long long h = 0;
-      uint32_t cnt = 0;
-      if (lane == 0) {
-        for (int side = 0; side < 2 && sd < 0; side++) {
-          const ReachSide& S = side ? s1 : s0;
-          if (!S.dq) continue;
-          for (int attempt = 0; attempt < 64; attempt++) {
-            const unsigned long long hh = slot_load(&S.ctr->pad[0]);
-            unsigned long long tt = slot_load(&S.ctr->pad[1]);
-            if (tt > kDonCap) tt = kDonCap;
-            if (hh >= tt) break;
-            const unsigned long long nh = hh + C < tt ? hh + C : tt;
-            if (atomicCAS(&S.ctr->pad[0], hh, nh) == hh) {
-              sd = side;
-              h = hh;
-              cnt = (uint32_t)(nh - hh);
-              break;
-            }
-          }
-        }
-      }
-      sd = __shfl_sync(kFull, sd, 0);
-      if (sd < 0) break;  // nothing to take: done
-      h = __shfl_sync(kFull, h, 0);
-      cnt = __shfl_sync(kFull, cnt, 0);
-      const ReachSide& S = sd ? s1 : s0;
-      uint32_t u = 0;
-      bool ok = true;
-      if (lane < cnt) {
-        const unsigned long long* slot = &S.dq[h + lane];
-        unsigned long long e = slot_load(slot);
-        for (uint32_t spin = 0; (uint32_t)(e >> 32) != tag && spin < kDonSpin; spin++)
-          e = slot_load(slot);
-        ok = (uint32_t)(e >> 32) == tag;
-        u = (uint32_t)e;
-      }
-      const uint32_t good = __ballot_sync(kFull, lane < cnt && ok);
-      if (good != (cnt == 32 ? kFull : ((1u << cnt) - 1))) lost = true;
-      // a slot that never showed its write is dropped (the launch reports
-      // it); the others move to the lowest lanes
-      const uint32_t n2 = __popc(good);
-      const unsigned src = __fns(good, 0, (int)lane + 1);
-      const uint32_t u2 = __shfl_sync(kFull, u, src < 32 ? src : 0);
-      run_chunk(sd, n2, lane < n2 ? u2 : 0u);
-    }
-  }
-
   if (lane == 0) {
     if (wv0) atomicAdd(&s0.ctr->waves, wv0);
     if (wv1) atomicAdd(&s1.ctr->waves, wv1);
-    if (lost) atomicOr(&s0.ctr->aux0, 1ull);
-  }
-  // the last warp to finish moves what is left in the queues to the next
-  // frontier (every other warp has written its slots and left)
-  if (s0.dq) {
-    __threadfence();
-    unsigned long long d = 0;
-    if (lane == 0) d = atomicAdd(&s0.ctr->aux1, 1ull);
-    d = __shfl_sync(kFull, d, 0);
-    if (d == nw - 1) {
-      __threadfence();
-      for (int sd = 0; sd < 2; sd++) {
-        const ReachSide& S = sd ? s1 : s0;
-        if (!S.dq) continue;
-        unsigned long long& nedges = sd ? nedges1 : nedges0;
-        const unsigned long long hh = slot_load(&S.ctr->pad[0]);
-        unsigned long long tt = slot_load(&S.ctr->pad[1]);
-        if (tt > kDonCap) tt = kDonCap;
-        for (unsigned long long b = hh; b < tt; b += 32) {
-          const unsigned long long i = b + lane;
-          bool take = false;
-          uint32_t v = 0;
-          if (i < tt) {
-            unsigned long long e = slot_load(&S.dq[i]);
-            for (uint32_t spin = 0; (uint32_t)(e >> 32) != tag && spin < kDonSpin; spin++)
-              e = slot_load(&S.dq[i]);
-            take = (uint32_t)(e >> 32) == tag;
-            if (!take) atomicOr(&s0.ctr->aux0, 1ull);
-            v = (uint32_t)e;
-          }
-          const unsigned long long pos = warp_append(&S.ctr->next, take);
-          if (take) {
-            S.qout[pos] = v;
-            nedges += S.off[v + 1] - S.off[v];
-          }
-        }
-      }
-    }
   }
   flush_side_counters(s0.ctr, s1.ctr, scanned0, scanned1, nedges0, nedges1, exp0, exp1);
 }
@@ -1147,42 +984,14 @@ static int vgc_occupancy(psc_graph_s* g) {
   return PSC_OK;
 }
 
-#ifndef PSC_VGC_DONATE
-#define PSC_VGC_DONATE 1
-#endif
-constexpr bool kVgcDonate = PSC_VGC_DONATE != 0;
-
-// The donation queues of a VGC launch: side k's slots at B_DQ + k * kDonCap,
-// zeroed once when allocated (a zero slot carries tag 0, which no launch
-// uses); a fresh tag per launch.
-static int donation_queues(psc_graph_s* g, ReachSide& a, ReachSide& b, uint32_t* tag) {
-  if (!kVgcDonate) return PSC_OK;
-  DevBuf& d = g->bufs[B_DQ];
-  const size_t bytes = 2ull * kDonCap * sizeof(unsigned long long);
-  if (d.bytes < bytes) {
-    void* p;
-    PSC_TRY(ensure(g, B_DQ, bytes, &p));
-    PSC_CUDA(cudaMemsetAsync(p, 0, bytes, g->stream));
-  }
-  unsigned long long* q = (unsigned long long*)d.p;
-  a.dq = a.ctr ? q : nullptr;
-  b.dq = b.ctr ? q + kDonCap : nullptr;
-  if (++g->vgc_tag == 0) ++g->vgc_tag;
-  *tag = g->vgc_tag;
-  return PSC_OK;
-}
-
-static int launch_vgc(psc_graph_s* g, unsigned blocks, ReachSide a, ReachSide b, uint32_t tau,
-                      uint32_t chunk) {
-  uint32_t tag = 0;
-  PSC_TRY(donation_queues(g, a, b, &tag));
+static void launch_vgc(psc_graph_s* g, unsigned blocks, const ReachSide& a, const ReachSide& b,
+                       uint32_t tau, uint32_t chunk) {
   if (vgc_narrow(g))
-    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow><<<blocks, kVgcBlock, 0, g->stream>>>(
-        a, b, tau, chunk, tag);
+    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow><<<blocks, kVgcBlock, 0, g->stream>>>(a, b, tau,
+                                                                                      chunk);
   else
-    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide><<<blocks, kVgcBlock, 0, g->stream>>>(
-        a, b, tau, chunk, tag);
-  return PSC_OK;
+    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide><<<blocks, kVgcBlock, 0, g->stream>>>(a, b, tau,
+                                                                                    chunk);
 }
 
 // Largest out-degree (out[0]) and in-degree (out[1]) of the graph.
@@ -1353,7 +1162,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           }
           {
             ProfScope ps(g, F_REACH_VGC);
-            PSC_TRY(launch_vgc(g, blocks, vg[0], vg[1], tau, 0u));
+            launch_vgc(g, blocks, vg[0], vg[1], tau, 0u);
           }
           if (heavy_possible) {
             // heavy vertices queued by this round (the kernel returns at once
@@ -1372,8 +1181,6 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           cudaEventElapsedTime(&t_ms, g->t0, e);
           give_event(g, e);
         }
-        for (int j = 0; j < kVgcChain; j++)  // a donated slot never written
-          if (g->hctr[chain_set(j, 0)].aux0) return PSC_ERR_ITER_LIMIT;
         for (int a = 0; a < na; a++) {
           Side& s = sides[act[a]];
           uint64_t nin = s.nf;
@@ -1447,13 +1254,8 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       const uint64_t max_warps = max_blocks * (kVgcBlock / 32);
       const uint64_t chunk = std::min<uint64_t>(32, (v_items + max_warps - 1) / max_warps);
       const uint64_t chunks = (v_items + chunk - 1) / chunk;
-      // with donation the whole resident grid runs: warps without a chunk
-      // take spilled vertices
-      const uint64_t blocks =
-          kVgcDonate ? max_blocks
-                     : std::min(max_blocks, (chunks + kVgcBlock / 32 - 1) / (kVgcBlock / 32));
-      PSC_TRY(launch_vgc(g, (unsigned)std::max<uint64_t>(1, blocks), vg[0], vg[1], tau,
-                         (uint32_t)chunk));
+      const uint64_t blocks = std::min(max_blocks, (chunks + kVgcBlock / 32 - 1) / (kVgcBlock / 32));
+      launch_vgc(g, (unsigned)std::max<uint64_t>(1, blocks), vg[0], vg[1], tau, (uint32_t)chunk);
     }
     if (np) {
       ProfScope ps(g, F_REACH_PUSH);
@@ -1545,7 +1347,6 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       if (mode[k] == M_NONE) continue;
       const Counters& c = g->hctr[s.cset];
       if (mode[k] == M_PULL && c.aux1) return PSC_ERR_ITER_LIMIT;  // a staged copy never came
-      if (mode[k] == M_VGC && c.aux0) return PSC_ERR_ITER_LIMIT;   // a donated slot never written
       if (g->profiling) {
         // algorithmic bytes: 16 per adjacency range read, 4 + 1 per edge
         // (target id, visited flag), 5 per new frontier vertex; pull: 16 per

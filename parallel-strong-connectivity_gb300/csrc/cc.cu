@@ -68,87 +68,82 @@ __global__ void k_ldd_centres(const uint32_t* __restrict__ perm, uint32_t start,
   }
 }
 
-// Push round: 32 frontier vertices per warp step, balanced expansion, K edges
-// in flight per lane; a neighbour is claimed with atomicCAS on its label.
-template <int BLOCK, int K>
+// Big frontier vertices of an LDD round (out-degree >= the VGC queue size),
+// listed by k_ldd_vgc with one 64-bit atomic on ctr->heavy = count <<
+// kLddPackShift | chunks that gives each entry (vertex << 32 | first chunk)
+// its slot and its first chunk of kLddChunk edges, increasing with the slot.
+// The chunks of all entries are cut into one contiguous range per warp of the
+// grid; a warp finds the entry of its first chunk once, then offers its
+// vertex's label to kLddChunk edges per step (atomicCAS from NONE, as in the
+// other LDD rounds).  A hub's edges are spread over the whole grid instead of
+// one warp.  Field widths: count < 2^30, chunks < 2^34 (m < 2^36).
+constexpr int kLddHeavyK = 4;
+constexpr uint64_t kLddChunk = 32 * kLddHeavyK;
+constexpr int kLddPackShift = 34;
+constexpr uint64_t kLddPackMask = (1ull << kLddPackShift) - 1;
+
+template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK)
-    k_ldd_push(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
-               const uint32_t* __restrict__ qin, uint64_t nin, uint32_t* label,
-               uint32_t* parent, uint32_t* qout, Counters* ctr) {
-  __shared__ WarpExpandSmem sm[BLOCK / 32];
-  __shared__ uint32_t s_lab[BLOCK];
-  __shared__ uint32_t s_u[BLOCK];
+    k_ldd_heavy(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
+                const uint64_t* __restrict__ big, uint32_t* label, uint32_t* parent,
+                uint32_t* qout, Counters* ctr) {
+  constexpr int K = kLddHeavyK;
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+  const unsigned long long packed = ctr->heavy;
+  const uint64_t nh = packed >> kLddPackShift, total = packed & kLddPackMask;
+  const uint64_t per = (total + nw - 1) / nw;
+  const uint64_t c_beg = gw * per, c_end = c_beg + per < total ? c_beg + per : total;
+  if (nh == 0 || c_beg >= c_end) return;
+  uint64_t h = 0, hi = nh - 1;  // last entry whose first chunk is <= c_beg
+  while (h < hi) {
+    const uint64_t mid = (h + hi + 1) >> 1;
+    if ((uint32_t)__ldg(&big[mid]) <= c_beg)
+      h = mid;
+    else
+      hi = mid - 1;
+  }
+  uint64_t ent = __ldg(&big[h]);
+  uint64_t cs = (uint32_t)ent, cn = h + 1 < nh ? (uint32_t)__ldg(&big[h + 1]) : total;
+  uint32_t u = (uint32_t)(ent >> 32), lu = label[u];
+  uint64_t beg = off[u], end = off[u + 1];
   unsigned long long scanned = 0, next_edges = 0;
-  for (uint64_t base = gw * 32; base < nin; base += nw * 32) {
-    const uint64_t i = base + lane;
-    uint64_t beg = 0, rem = 0;
-    uint32_t u = 0, lu = 0;
-    if (i < nin) {
-      u = qin[i];
-      beg = off[u];
-      rem = off[u + 1] - beg;
+  for (uint64_t c = c_beg; c < c_end; c++) {
+    if (c >= cn) {
+      h++;
+      ent = __ldg(&big[h]);
+      cs = cn;
+      cn = h + 1 < nh ? (uint32_t)__ldg(&big[h + 1]) : total;
+      u = (uint32_t)(ent >> 32);
       lu = label[u];
+      beg = off[u];
+      end = off[u + 1];
     }
-    scanned += rem;
-    s_lab[wid * 32 + lane] = lu;
-    s_u[wid * 32 + lane] = u;
-    // adjacency lists in pieces of at most 2^26 edges (32-bit warp scan)
-    while (__any_sync(kFull, rem > 0)) {
-      const uint32_t deg = (uint32_t)(rem < (1ull << 26) ? rem : (1ull << 26));
-      uint32_t incl = deg;
+    const uint64_t e0 = beg + (c - cs) * kLddChunk;
+    uint32_t v[K], tm = 0, pre = 0;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(kFull, incl, o);
-        if ((int)lane >= o) incl += t;
+    for (int k = 0; k < K; k++) {
+      const uint64_t e = e0 + k * 32 + lane;
+      v[k] = kNone;
+      if (e < end) {
+        scanned++;
+        v[k] = __ldg(&E[e]);
       }
-      const uint32_t total = __shfl_sync(kFull, incl, 31);
-      sm[wid].excl[lane] = incl - deg;
-      sm[wid].beg[lane] = beg;
-      __syncwarp();
-      for (uint32_t b = 0; b < total; b += 32 * K) {
-        uint32_t v[K], src[K], tm = 0;
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-          const uint32_t gi = b + k * 32 + lane;
-          v[k] = kNone;
-          src[k] = 0;
-          if (gi < total) {
-            int lo = 0, hi = 31;
-            while (lo < hi) {
-              const int mid = (lo + hi + 1) >> 1;
-              if (sm[wid].excl[mid] <= gi)
-                lo = mid;
-              else
-                hi = mid - 1;
-            }
-            src[k] = lo;
-            v[k] = __ldg(&E[sm[wid].beg[lo] + (gi - sm[wid].excl[lo])]);
-          }
-        }
-        uint32_t pre = 0;
-#pragma unroll
-        for (int k = 0; k < K; k++)
-          if (v[k] != kNone && __ldcg(&label[v[k]]) == kNone) pre |= 1u << k;
-#pragma unroll
-        for (int k = 0; k < K; k++)
-          if (pre & (1u << k)) {
-            if (atomicCAS(&label[v[k]], kNone, s_lab[wid * 32 + src[k]]) == kNone) {
-              tm |= 1u << k;
-              if (parent) parent[v[k]] = s_u[wid * 32 + src[k]];
-            }
-          }
-        warp_append_batch<K>(tm, v, qout, &ctr->next);
-#pragma unroll
-        for (int k = 0; k < K; k++)
-          if (tm & (1u << k)) next_edges += off[v[k] + 1] - off[v[k]];
-      }
-      __syncwarp();
-      beg += deg;
-      rem -= deg;
     }
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (v[k] != kNone && __ldcg(&label[v[k]]) == kNone) pre |= 1u << k;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if ((pre & (1u << k)) && atomicCAS(&label[v[k]], kNone, lu) == kNone) {
+        tm |= 1u << k;
+        if (parent) parent[v[k]] = u;
+      }
+    warp_append_batch<K>(tm, v, qout, &ctr->next);
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (tm & (1u << k)) next_edges += off[v[k] + 1] - off[v[k]];
   }
   scanned = warp_sum(scanned);
   next_edges = warp_sum(next_edges);
@@ -168,7 +163,7 @@ __global__ void __launch_bounds__(BLOCK)
 // vertices it claims in the queue while there is room and spills the rest to
 // the next frontier, as is whatever is left when the queue fills.  Queued
 // vertices with deg > tq spill too; chunk vertices with deg >= tq go to the
-// `big` list, which the balanced push kernel expands afterwards.
+// `big` list, whose edges k_ldd_heavy spreads over the grid afterwards.
 constexpr int kLddQueue = 512;
 constexpr int kLddVgcBlock = 128;
 constexpr int kLddK = 8;
@@ -183,7 +178,7 @@ template <int BLOCK, int QCAP>
 __global__ void __launch_bounds__(BLOCK)
     k_ldd_vgc(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
               const uint32_t* __restrict__ qin, uint64_t nin, uint32_t* label, uint32_t* parent,
-              uint32_t* qout, uint32_t* big, uint32_t tau, uint32_t chunk, Counters* ctr) {
+              uint32_t* qout, uint64_t* big, uint32_t tau, uint32_t chunk, Counters* ctr) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ LEnt sq[BLOCK / 32][QCAP];
   __shared__ uint32_t slab[BLOCK / 32][QCAP];
@@ -209,10 +204,10 @@ __global__ void __launch_bounds__(BLOCK)
       du = off[u + 1] - ub;
       lu = label[u];
     }
-    const bool isbig = lane < cnt && du >= tq;
-    {
-      const unsigned long long pos = warp_append(&ctr->heavy, isbig);
-      if (isbig) big[pos] = u;
+    if (lane < cnt && du >= tq) {
+      const unsigned long long old = atomicAdd(
+          &ctr->heavy, (1ull << kLddPackShift) + (du + kLddChunk - 1) / kLddChunk);
+      big[old >> kLddPackShift] = ((uint64_t)u << 32) | (old & kLddPackMask);
     }
     const bool seed = lane < cnt && du > 0 && du < tq;
     const uint32_t smask = __ballot_sync(kFull, seed);
@@ -632,6 +627,7 @@ static void ldd_members(const psc_graph_s* g, std::vector<uint64_t>& base,
 // the centre list is laid out sample-major: entry i * G + k.
 int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
   const uint64_t n = g->n, m = g->m, nwords = (n + 31) / 32;
+  if (m >> 36) return PSC_ERR_TOO_LARGE;  // big-list fields (k_ldd_heavy)
   const unsigned tb = kCcBlock;
   std::vector<uint64_t> mb, ms;
   ldd_members(g, mb, ms);
@@ -699,7 +695,8 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
     PSC_TRY(zero_counters(g));
     if (!pull) {
       // VGC round on a resident grid, then the big-degree frontier vertices
-      // it set aside, expanded by the balanced push kernel into the same queue
+      // it set aside, their edges cut into chunks over the whole grid, into
+      // the same queue
       if (!g->ldd_vgc_blocks) {
         PSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &g->ldd_vgc_blocks, k_ldd_vgc<kLddVgcBlock, kLddQueue>, kLddVgcBlock, 0));
@@ -711,7 +708,7 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
       const uint64_t chunks = (nf + chunk - 1) / chunk;
       const uint64_t blocks =
           std::min(max_blocks, (chunks + kLddVgcBlock / 32 - 1) / (kLddVgcBlock / 32));
-      uint32_t* big;
+      uint64_t* big;
       PSC_TRY(ensure_t(g, B_HEAVY, n + 1, &big));
       {
         ProfScope ps(g, F_CC);
@@ -721,11 +718,10 @@ int ldd_run(psc_graph_s* g, double beta, uint32_t* d_label, uint32_t* tree) {
       }
       PSC_CUDA(cudaGetLastError());
       PSC_TRY(read_counters(g));
-      const uint64_t nbig = g->hctr[0].heavy;
-      if (nbig) {
+      if (g->hctr[0].heavy >> kLddPackShift) {
         ProfScope ps(g, F_CC);
-        k_ldd_push<kCcBlock, 4><<<grid_for(g, nbig, tb), tb, 0, g->stream>>>(
-            g->off, g->E, big, nbig, d_label, tree, qb, g->ctr);
+        k_ldd_heavy<kCcBlock><<<g->num_sms * 4, kCcBlock, 0, g->stream>>>(
+            g->off, g->E, big, d_label, tree, qb, g->ctr);
       }
       std::swap(qa, qb);
       swap_bufs(g, B_QA, B_QB);

@@ -255,26 +255,23 @@ __device__ __forceinline__ void vgc_place(uint32_t tm, const uint32_t* w, const 
 }
 
 // Claims of one batch: a claimed vertex enters the queue with its adjacency
-// range, so the next wave needs no dependent load.  With PSC_VGC_SPEC the
-// range is loaded alongside the claim (speculatively: wasted traffic when the
-// claim fails, but off the claim's latency chain); without it, only after a
-// claim succeeds.
-#ifndef PSC_VGC_SPEC
-#define PSC_VGC_SPEC 1
-#endif
-template <int K>
+// range, so the next wave needs no dependent load.  SPEC: the range is loaded
+// alongside the claim (off the claim's latency chain, but wasted traffic when
+// the claim fails), for latency-bound rounds; otherwise only after a claim
+// succeeds, for rounds with more frontier than resident warps.
+template <int K, bool SPEC>
 __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, uint64_t* ve,
                                               const uint64_t* __restrict__ off, uint32_t* vis) {
-#if PSC_VGC_SPEC
+  if (SPEC) {
 #pragma unroll
-  for (int k = 0; k < K; k++) {
-    vb[k] = ve[k] = 0;
-    if (w[k] != 0xFFFFFFFFu) {
-      vb[k] = __ldg(&off[w[k]]);
-      ve[k] = __ldg(&off[w[k] + 1]);
+    for (int k = 0; k < K; k++) {
+      vb[k] = ve[k] = 0;
+      if (w[k] != 0xFFFFFFFFu) {
+        vb[k] = __ldg(&off[w[k]]);
+        ve[k] = __ldg(&off[w[k] + 1]);
+      }
     }
   }
-#endif
   uint32_t tm = 0;
 #pragma unroll
   for (int k = 0; k < K; k++)
@@ -282,16 +279,16 @@ __device__ __forceinline__ uint32_t vgc_claim(const uint32_t* w, uint64_t* vb, u
       const uint32_t b = 1u << (w[k] & 31);
       if (!(atomicOr(&vis[w[k] >> 5], b) & b)) tm |= 1u << k;
     }
-#if !PSC_VGC_SPEC
+  if (!SPEC) {
 #pragma unroll
-  for (int k = 0; k < K; k++) {
-    vb[k] = ve[k] = 0;
-    if (tm & (1u << k)) {
-      vb[k] = __ldg(&off[w[k]]);
-      ve[k] = __ldg(&off[w[k] + 1]);
+    for (int k = 0; k < K; k++) {
+      vb[k] = ve[k] = 0;
+      if (tm & (1u << k)) {
+        vb[k] = __ldg(&off[w[k]]);
+        ve[k] = __ldg(&off[w[k] + 1]);
+      }
     }
   }
-#endif
   return tm;
 }
 
@@ -331,7 +328,7 @@ __device__ __forceinline__ void vgc_direct(const ReachSide& S, uint64_t ub, uint
 // out-edges, and whatever is left in the queue when it fills or after
 // max_waves waves, are spilled too.
 // Other chunk vertices are expanded directly (heavy ones by the whole grid).
-template <int BLOCK, int QCAP, int K>
+template <int BLOCK, int QCAP, int K, bool SPEC>
 __global__ void __launch_bounds__(BLOCK)
     k_reach_vgc(ReachSide s0, ReachSide s1, uint32_t tau, uint32_t chunk) {
   __shared__ WarpExpandSmem sm[BLOCK / 32];
@@ -439,7 +436,7 @@ __global__ void __launch_bounds__(BLOCK)
             w[k] = __ldg(&S.E[sm[wid].beg[src] + (gi - sm[wid].excl[src])]);
           }
         }
-        const uint32_t tm = vgc_claim<K>(w, vb, ve, S.off, S.vis);
+        const uint32_t tm = vgc_claim<K, SPEC>(w, vb, ve, S.off, S.vis);
         vgc_place<K>(tm, w, vb, ve, Q, tail, tq, S.qout, &S.ctr->next, nedges);
       }
     }
@@ -974,24 +971,32 @@ static bool vgc_narrow(const psc_graph_s* g) { return g->m < 8 * g->n; }
 static int vgc_occupancy(psc_graph_s* g) {
   if (!g->vgc_blocks) {
     PSC_CUDA(vgc_narrow(g) ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                                 &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow>,
+                                 &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow, true>,
                                  kVgcBlock, 0)
                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                                 &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide>,
+                                 &g->vgc_blocks, k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide, true>,
                                  kVgcBlock, 0));
     if (g->vgc_blocks < 1) g->vgc_blocks = 1;
   }
   return PSC_OK;
 }
 
+// spec: speculative range loads (vgc_claim), for rounds whose frontier fits
+// the resident grid one vertex per warp
 static void launch_vgc(psc_graph_s* g, unsigned blocks, const ReachSide& a, const ReachSide& b,
-                       uint32_t tau, uint32_t chunk) {
-  if (vgc_narrow(g))
-    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow><<<blocks, kVgcBlock, 0, g->stream>>>(a, b, tau,
-                                                                                      chunk);
-  else
-    k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide><<<blocks, kVgcBlock, 0, g->stream>>>(a, b, tau,
-                                                                                    chunk);
+                       uint32_t tau, uint32_t chunk, bool spec) {
+  cudaStream_t st = g->stream;
+  if (vgc_narrow(g)) {
+    if (spec)
+      k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow, true><<<blocks, kVgcBlock, 0, st>>>(a, b, tau, chunk);
+    else
+      k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKNarrow, false><<<blocks, kVgcBlock, 0, st>>>(a, b, tau, chunk);
+  } else {
+    if (spec)
+      k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide, true><<<blocks, kVgcBlock, 0, st>>>(a, b, tau, chunk);
+    else
+      k_reach_vgc<kVgcBlock, kVgcQueue, kVgcKWide, false><<<blocks, kVgcBlock, 0, st>>>(a, b, tau, chunk);
+  }
 }
 
 // Largest out-degree (out[0]) and in-degree (out[1]) of the graph.
@@ -1146,6 +1151,11 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           heavy_possible |= g->max_deg[sides[act[a]].backward ? 1 : 0] > kHeavyDeg;
         PSC_TRY(vgc_occupancy(g));
         const unsigned blocks = (unsigned)((uint64_t)g->num_sms * g->vgc_blocks);
+        // speculative range loads while the frontier fits the grid one
+        // vertex per warp (steady frontiers stay near their start size)
+        uint64_t chain_nf = 0;
+        for (int a = 0; a < na; a++) chain_nf += sides[act[a]].nf;
+        const bool spec = chain_nf <= (uint64_t)blocks * (kVgcBlock / 32);
         PSC_TRY(zero_counters(g));
         for (int j = 0; j < kVgcChain; j++) {
           ReachSide vg[2] = {};
@@ -1162,7 +1172,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           }
           {
             ProfScope ps(g, F_REACH_VGC);
-            launch_vgc(g, blocks, vg[0], vg[1], tau, 0u);
+            launch_vgc(g, blocks, vg[0], vg[1], tau, 0u, spec);
           }
           if (heavy_possible) {
             // heavy vertices queued by this round (the kernel returns at once
@@ -1255,7 +1265,8 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       const uint64_t chunk = std::min<uint64_t>(32, (v_items + max_warps - 1) / max_warps);
       const uint64_t chunks = (v_items + chunk - 1) / chunk;
       const uint64_t blocks = std::min(max_blocks, (chunks + kVgcBlock / 32 - 1) / (kVgcBlock / 32));
-      launch_vgc(g, (unsigned)std::max<uint64_t>(1, blocks), vg[0], vg[1], tau, (uint32_t)chunk);
+      launch_vgc(g, (unsigned)std::max<uint64_t>(1, blocks), vg[0], vg[1], tau, (uint32_t)chunk,
+                 chunk == 1);
     }
     if (np) {
       ProfScope ps(g, F_REACH_PUSH);
@@ -1336,11 +1347,11 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       for (int k = 0; k < ns; k++)
         if (mode[k] != M_NONE)
           std::fprintf(stderr, "reach side %d round %u mode %s nf %llu next %llu edges %llu "
-                       "expanded %llu waves %llu t %.3f ms\n",
+                       "expanded %llu unvisited %llu waves %llu t %.3f ms\n",
                        k, sides[k].rounds, mode[k] == M_VGC ? "vgc" : mode[k] == M_PUSH ? "push" : "pull",
                        (unsigned long long)sides[k].nf, g->hctr[sides[k].cset].next,
                        g->hctr[sides[k].cset].edges, g->hctr[sides[k].cset].expanded,
-                       g->hctr[sides[k].cset].waves, us);
+                       g->hctr[sides[k].cset].unvisited, g->hctr[sides[k].cset].waves, us);
     }
     for (int k = 0; k < ns; k++) {
       Side& s = sides[k];

@@ -115,6 +115,8 @@ struct psc_graph_s {
   int ldd_vgc_blocks = 0; // same for the LDD VGC kernel
   int le_heavy_blocks = 0; // same for the LE-list heavy-pair kernel
   bool deg_known = false;    // max_deg holds the largest out- / in-degree
+  bool dead_known = false;   // B_DEAD holds the unreachable-vertex bitmaps
+  uint64_t dead_count[2] = {0, 0};  // vertices with no in-edge / no out-edge
   // per LDD round of the last psc_ldd / psc_cc call: first candidate index,
   // candidates offered, new centres (psc_ldd_rounds)
   std::vector<uint32_t> ldd_trace;
@@ -183,6 +185,7 @@ enum Buf : int {
   B_FLAB,         // u32 labels of a batch's pivots
   B_SCHED,        // window schedule of a batch's prefix-doubling rounds
   B_SCANBITS,     // u32[n/32] selection bits of scan_emit_flags
+  B_DEAD,         // u32[2][n/32 + 1] vertices with no in-edge, then no out-edge
   B_COUNT
 };
 

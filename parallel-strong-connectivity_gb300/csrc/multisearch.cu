@@ -82,17 +82,22 @@ struct MsSrc {
   uint32_t fail;
 };
 
+// Seeds both sides of a batch: pair (front[i], label) into each side's table
+// and frontier.
 __global__ void k_ms_seed(const uint32_t* __restrict__ front, uint64_t nf, uint64_t label_offset,
-                          const uint32_t* __restrict__ front_labels, unsigned long long* T,
-                          uint64_t mask, uint64_t* F, const unsigned long long* nf_dev) {
+                          const uint32_t* __restrict__ front_labels, unsigned long long* T0,
+                          uint64_t mask0, uint64_t* F0, unsigned long long* T1, uint64_t mask1,
+                          uint64_t* F1, const unsigned long long* nf_dev) {
   if (nf_dev) nf = *nf_dev;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t lab = front_labels ? front_labels[i] : (uint32_t)(label_offset + i);
-    uint64_t key = ((uint64_t)front[i] << 32) | (uint64_t)lab;
+    const uint64_t key = ((uint64_t)front[i] << 32) | (uint64_t)lab;
     uint32_t pr = 0;
-    table_insert(T, mask, key, (uint32_t)(mask + 1 < 0xFFFFFFFFull ? mask + 1 : 0xFFFFFFFFu), &pr);
-    F[i] = key;
+    table_insert(T0, mask0, key, (uint32_t)(mask0 + 1 < 0xFFFFFFFFull ? mask0 + 1 : 0xFFFFFFFFu), &pr);
+    table_insert(T1, mask1, key, (uint32_t)(mask1 + 1 < 0xFFFFFFFFull ? mask1 + 1 : 0xFFFFFFFFu), &pr);
+    F0[i] = key;
+    F1[i] = key;
   }
 }
 
@@ -774,14 +779,16 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
     PSC_TRY(ensure(g, s.b_slot, s.cap * 8 + 16, &q));
     PSC_TRY(ensure(g, s.h_slot, s.cap * 8 + 16, &q));
     PSC_TRY(ensure(g, s.f_slot, s.cap * 4 + 16, &q));
-    {
-      ProfScope ps(g, F_MS_SEED);
-      ps.bytes = 20.0 * n_front;
-      k_ms_seed<<<grid_for(g, n_front, 256), 256, 0, g->stream>>>(
-          front, n_front, label_offset, front_labels, (unsigned long long*)g->bufs[s.t_slot].p,
-          s.cap - 1, (uint64_t*)g->bufs[s.a_slot].p, async ? async->nf_dev : nullptr);
-    }
     s.nf = s.ne = n_front;
+  }
+  {
+    ProfScope ps(g, F_MS_SEED);
+    ps.bytes = 40.0 * n_front;
+    k_ms_seed<<<grid_for(g, n_front, 256), 256, 0, g->stream>>>(
+        front, n_front, label_offset, front_labels, (unsigned long long*)g->bufs[st[0].t_slot].p,
+        st[0].cap - 1, (uint64_t*)g->bufs[st[0].a_slot].p,
+        (unsigned long long*)g->bufs[st[1].t_slot].p, st[1].cap - 1,
+        (uint64_t*)g->bufs[st[1].a_slot].p, async ? async->nf_dev : nullptr);
   }
   // asynchronous start: the first sub-round runs on the device's pivot count
   // and the heavy walk follows it whenever some vertex could be heavy

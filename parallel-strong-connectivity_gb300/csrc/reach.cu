@@ -663,19 +663,27 @@ __device__ __forceinline__ void flush_pull_counters(Counters* ctr, unsigned long
 }
 
 // A warp's W words read from global memory: visited words and in-list ranges.
+// dead (optional): bitmap of vertices without in-edges in this direction,
+// which no pull can reach; they are skipped like visited ones (no in-list
+// range read) but keep their visited bit clear.
 template <int W>
 __device__ __forceinline__ void pull_load_global(uint64_t w, uint64_t nwords, uint64_t n,
                                                  const uint64_t* __restrict__ B_off,
+                                                 const uint32_t* __restrict__ dead,
                                                  const uint32_t* vis, uint32_t* vw, bool* t,
                                                  uint64_t* b, uint64_t* e,
                                                  unsigned long long& unvisited) {
   const unsigned lane = lane_id();
+  uint32_t dw[W];
 #pragma unroll
-  for (int k = 0; k < W; k++) vw[k] = w + k < nwords ? vis[w + k] : ~0u;
+  for (int k = 0; k < W; k++) {
+    vw[k] = w + k < nwords ? vis[w + k] : ~0u;
+    dw[k] = dead && w + k < nwords ? __ldg(&dead[w + k]) : 0u;
+  }
 #pragma unroll
   for (int k = 0; k < W; k++) {
     const uint64_t v = (w + k) * 32 + lane;
-    t[k] = v < n && !((vw[k] >> lane) & 1u);
+    t[k] = v < n && !(((vw[k] | dw[k]) >> lane) & 1u);
     b[k] = e[k] = 0;
     if (t[k]) {
       b[k] = B_off[v];
@@ -693,7 +701,7 @@ template <int BLOCK, int W>
 __global__ void __launch_bounds__(BLOCK)
     k_reach_pull(const uint64_t* __restrict__ B_off, const uint32_t* __restrict__ B_E,
                  const uint32_t* __restrict__ fb_in, uint32_t* vis, uint32_t* fb_out, uint64_t n,
-                 Counters* ctr) {
+                 Counters* ctr, const uint32_t* __restrict__ dead) {
   const unsigned wid = threadIdx.x >> 5;
   const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
   const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
@@ -703,7 +711,7 @@ __global__ void __launch_bounds__(BLOCK)
     uint32_t vw[W];
     bool t[W];
     uint64_t b[W], e[W];
-    pull_load_global<W>(w, nwords, n, B_off, vis, vw, t, b, e, unvisited);
+    pull_load_global<W>(w, nwords, n, B_off, dead, vis, vw, t, b, e, unvisited);
     pull_step<W>(w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
   }
   flush_pull_counters(ctr, cnt, scanned, unvisited);
@@ -839,7 +847,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK)
         pending |= 1u << buf;
       }
     } else {
-      pull_load_global<W>(w, nwords, n, B_off, vis, vw, t, b, e, unvisited);
+      pull_load_global<W>(w, nwords, n, B_off, nullptr, vis, vw, t, b, e, unvisited);
     }
     pull_step<W>(w, nwords, vw, t, b, e, B_E, fb_in, vis, fb_out, cnt, scanned);
   }
@@ -1036,6 +1044,44 @@ int max_degrees_once(psc_graph_s* g) {
   return PSC_OK;
 }
 
+// Bitmap words of vertices whose range in off is empty (one warp per word),
+// and their count.
+__global__ void k_dead_bits(const uint64_t* __restrict__ off, uint64_t n, uint32_t* bits,
+                            unsigned long long* count) {
+  const uint64_t nwords = (n + 31) >> 5;
+  unsigned long long c = 0;
+  for (uint64_t base = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ull;
+       base < nwords * 32; base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v = base + lane_id();
+    const uint32_t word = __ballot_sync(kFull, v < n && off[v + 1] == off[v]);
+    if (lane_id() == 0) {
+      bits[base >> 5] = word;
+      c += __popc(word);
+    }
+  }
+  if (lane_id() == 0 && c) atomicAdd(count, c);
+}
+
+// Once per handle: the vertices a forward pull can never reach (no in-edge)
+// and those a backward pull can never reach (no out-edge).
+static int dead_bits_once(psc_graph_s* g) {
+  if (g->dead_known) return PSC_OK;
+  const uint64_t nwords = (g->n + 31) / 32;
+  uint32_t* d;
+  PSC_TRY(ensure_t(g, B_DEAD, 2 * (nwords + 1), &d));
+  unsigned long long* c = &g->ctr[2].aux0;  // aux0, aux1 of the staging set
+  PSC_CUDA(cudaMemsetAsync(c, 0, 2 * sizeof(unsigned long long), g->stream));
+  k_dead_bits<<<grid_for(g, nwords * 32, 256), 256, 0, g->stream>>>(g->in_off, g->n, d, c);
+  k_dead_bits<<<grid_for(g, nwords * 32, 256), 256, 0, g->stream>>>(g->off, g->n, d + nwords + 1,
+                                                                     c + 1);
+  PSC_CUDA(cudaGetLastError());
+  PSC_TRY(read_counters(g));
+  g->dead_count[0] = g->hctr[2].aux0;
+  g->dead_count[1] = g->hctr[2].aux1;
+  g->dead_known = true;
+  return PSC_OK;
+}
+
 struct Side {
   bool backward = false;
   uint32_t* vis = nullptr;
@@ -1044,6 +1090,10 @@ struct Side {
   uint64_t nf = 0, nf_edges = 0, prev_nf = 0;
   bool pull = false;
   uint32_t rounds = 0;
+  // unvisited vertices that some pull could still reach, after the last
+  // pull round (an upper bound; UINT64_MAX before the first)
+  uint64_t live = UINT64_MAX;
+  bool staged = false;  // the last pull round ran the staged kernel (counts dead vertices)
 };
 
 // Chained VGC rounds (see reach_sides): rounds per chain, and the counter set
@@ -1227,6 +1277,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       uint32_t* qa = (uint32_t*)g->bufs[s.slot_qa].p;
       uint32_t* fa = (uint32_t*)g->bufs[s.slot_fa].p;
       if (want_pull && !s.pull) {
+        PSC_TRY(dead_bits_once(g));
         ProfScope ps(g, F_REACH_PULL);
         PSC_CUDA(cudaMemsetAsync(fa, 0, nwords * 4, g->stream));
         k_queue_to_bitmap<<<grid_for(g, s.nf, 256), 256, 0, g->stream>>>(qa, s.nf, fa);
@@ -1291,27 +1342,36 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       const uint64_t* A_off = s.backward ? g->in_off : g->off;
       const uint32_t* fa = (const uint32_t*)g->bufs[s.slot_fa].p;
       uint32_t* fbo = (uint32_t*)g->bufs[s.slot_fb].p;
+      const uint32_t* dead = (const uint32_t*)g->bufs[B_DEAD].p + (s.backward ? nwords + 1 : 0);
+      // Few vertices left that a pull could reach (on R-MAT 2^26 the second
+      // pull round finds 1-2 M of the 41 M unvisited, the rest have no
+      // in-edge): the global-memory kernel with the dead bitmap reads only
+      // their ranges, where the staged one copies every range.
+      const bool sparse = s.live != UINT64_MAX && 8 * s.live < n;
+      s.staged = false;
       switch (g->block) {
         case 128:
           k_reach_pull<128, kPullW><<<pull_grid<128>(g->num_sms, nwords), 128, 0, g->stream>>>(
-              B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
+              B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset, dead);
           break;
         case 512:
           k_reach_pull<512, kPullW><<<pull_grid<512>(g->num_sms, nwords), 512, 0, g->stream>>>(
-              B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
+              B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset, dead);
           break;
         default:
           // staged tiles when at least one tile fits inside the arrays and
           // they are 16-byte aligned (bulk copies)
-          if (kPullStaged && n >= kPullStagedTile + 1 && ((uintptr_t)B_off & 15) == 0 &&
-              ((uintptr_t)s.vis & 15) == 0)
+          if (kPullStaged && !sparse && n >= kPullStagedTile + 1 && ((uintptr_t)B_off & 15) == 0 &&
+              ((uintptr_t)s.vis & 15) == 0) {
+            s.staged = true;
             k_reach_pull_staged<kReachBlock, kPullW>
                 <<<pull_grid<kReachBlock, true>(g->num_sms, nwords), kReachBlock, 0, g->stream>>>(
                     B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
-          else
+          } else {
             k_reach_pull<kReachBlock, kPullW>
                 <<<pull_grid<kReachBlock>(g->num_sms, nwords), kReachBlock, 0, g->stream>>>(
-                    B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
+                    B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset, dead);
+          }
       }
       k_pull_out_edges<<<grid_for(g, nwords, 256), 256, 0, g->stream>>>(
           fbo, A_off, n, hash32((uint32_t)s.rounds), g->ctr + s.cset);
@@ -1367,6 +1427,12 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
         g->prof[fam].bytes += mode[k] == M_PULL
                                   ? 16.0 * c.unvisited + 5.0 * c.edges + 0.25 * n + 1.0 * c.next
                                   : 16.0 * c.expanded + 5.0 * c.edges + 5.0 * c.next;
+      }
+      if (mode[k] == M_PULL) {
+        // unvisited minus found, minus the dead ones when the kernel counted them
+        const uint64_t dead_n = s.staged ? g->dead_count[s.backward ? 1 : 0] : 0;
+        const uint64_t u = c.unvisited > dead_n ? c.unvisited - dead_n : 0;
+        s.live = u > c.next ? u - c.next : 0;
       }
       if (mode[k] == M_PULL)
         std::swap(g->bufs[s.slot_fa], g->bufs[s.slot_fb]);
@@ -1578,7 +1644,7 @@ extern "C" int psc_reach_noalloc(const uint64_t* d_off, const uint32_t* d_E,
     } else {
       k_reach_pull<kReachBlock, kPullW>
           <<<pull_grid<kReachBlock>(nd.num_sms, nwords), kReachBlock, 0, s>>>(
-              B_off, B_E, fa, vis, fb, n, ctr);
+              B_off, B_E, fa, vis, fb, n, ctr, nullptr);
       k_pull_out_edges<<<na_grid(nd.num_sms, nwords, 256), 256, 0, s>>>(fb, A_off, n,
                                                                         hash32(r), ctr);
       std::swap(fa, fb);

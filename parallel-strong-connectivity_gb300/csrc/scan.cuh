@@ -166,6 +166,28 @@ __global__ void __launch_bounds__(kScanBlock) k_flag_tile_sum(Value value, uint6
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
 }
 
+// scan_emit_flags of at most one tile in one launch: flags, scan, emits and
+// the total (written to *total).
+template <class Value, class Emit>
+__global__ void __launch_bounds__(kScanBlock) k_flag_emit_tile(Value value, Emit emit, uint64_t n,
+                                                               uint64_t* total) {
+  __shared__ uint64_t sm[kScanItems * kScanBlock / 32 + 1];
+  uint32_t v[kScanItems];
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    const uint64_t i = (uint64_t)k * kScanBlock + threadIdx.x;
+    v[k] = i < n ? value(i) : 0u;
+  }
+  uint64_t ex[kScanItems], tot;
+  block_scan_striped<kScanBlock, kScanItems>(v, ex, sm, &tot);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    const uint64_t i = (uint64_t)k * kScanBlock + threadIdx.x;
+    if (i < n) emit(i, ex[k], v[k]);
+  }
+  if (threadIdx.x == 0) *total = tot;
+}
+
 struct BitValue {
   const uint32_t* bits;
   __device__ uint32_t operator()(uint64_t i) const { return (bits[i >> 5] >> (i & 31)) & 1u; }
@@ -220,20 +242,25 @@ int scan_emit_flags(psc_graph_s* g, uint64_t n, Value value, Emit emit, uint64_t
   }
   const uint64_t ntiles = (n + kScanTile - 1) / kScanTile;
   uint64_t* ts = nullptr;
-  uint32_t* bits = nullptr;
   PSC_TRY(ensure_t(g, B_SCAN, ntiles + 2, &ts));
-  PSC_TRY(ensure_t(g, B_SCANBITS, (n + 31) / 32 + 1, &bits));
-  {
+  if (ntiles == 1) {
     ProfScope ps(g, fam);
-    k_flag_tile_sum<<<(unsigned)ntiles, kScanBlock, 0, g->stream>>>(value, n, ts, bits);
-  }
-  {
-    ProfScope ps(g, fam);
-    k_scan_tile_sums<<<1, 1024, 0, g->stream>>>(ts, ntiles);
-  }
-  {
-    ProfScope ps(g, fam);
-    k_tile_emit<<<(unsigned)ntiles, kScanBlock, 0, g->stream>>>(BitValue{bits}, emit, n, ts);
+    k_flag_emit_tile<<<1, kScanBlock, 0, g->stream>>>(value, emit, n, ts + 1);
+  } else {
+    uint32_t* bits = nullptr;
+    PSC_TRY(ensure_t(g, B_SCANBITS, (n + 31) / 32 + 1, &bits));
+    {
+      ProfScope ps(g, fam);
+      k_flag_tile_sum<<<(unsigned)ntiles, kScanBlock, 0, g->stream>>>(value, n, ts, bits);
+    }
+    {
+      ProfScope ps(g, fam);
+      k_scan_tile_sums<<<1, 1024, 0, g->stream>>>(ts, ntiles);
+    }
+    {
+      ProfScope ps(g, fam);
+      k_tile_emit<<<(unsigned)ntiles, kScanBlock, 0, g->stream>>>(BitValue{bits}, emit, n, ts);
+    }
   }
   PSC_CUDA(cudaGetLastError());
   if (total_dev) *total_dev = (const unsigned long long*)(ts + ntiles);

@@ -75,29 +75,22 @@ __global__ void k_label_first(const uint32_t* __restrict__ vf, const uint32_t* _
   }
 }
 
-__global__ void k_partition_small(const unsigned long long* __restrict__ Ts, uint64_t cap_s,
-                                  const unsigned long long* __restrict__ Tl, uint64_t mask_l,
-                                  unsigned long long* labels) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap_s;
+// Partition (scc.hpp:437-464) of one batch in one launch: items below cap_s
+// are slots of the smaller table, whose pairs also found in the larger table
+// get their label with kTopBit (reached both ways); the rest are slots of the
+// larger table.  Every write is an atomicMax, so the order does not matter.
+__global__ void k_partition(const unsigned long long* __restrict__ Ts, uint64_t cap_s,
+                            const unsigned long long* __restrict__ Tl, uint64_t cap_l,
+                            unsigned long long* labels) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap_s + cap_l;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t e = Ts[i];
+    const bool small = i < cap_s;
+    const uint64_t e = small ? Ts[i] : Tl[i - cap_s];
     if (e == kEmpty) continue;
     const uint32_t v = (uint32_t)(e >> 32);
     const uint64_t l = e & kValMask;
-    const uint64_t val = table_contains(Tl, mask_l, e) ? (l | kTopBit) : l;
+    const uint64_t val = small && table_contains(Tl, cap_l - 1, e) ? (l | kTopBit) : l;
     if (labels[v] < val) atomicMax(&labels[v], (unsigned long long)val);
-  }
-}
-
-__global__ void k_partition_large(const unsigned long long* __restrict__ Tl, uint64_t cap_l,
-                                  unsigned long long* labels) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap_l;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t e = Tl[i];
-    if (e == kEmpty) continue;
-    const uint32_t v = (uint32_t)(e >> 32);
-    const uint64_t l = e & kValMask;
-    if (labels[v] < l) atomicMax(&labels[v], (unsigned long long)l);
   }
 }
 
@@ -153,15 +146,10 @@ int scc_partition(psc_graph_s* g, const MsResult res[2], uint64_t* labels) {
   const uint64_t cap_s = f_small ? rf.cap : rb.cap, cap_l = f_small ? rb.cap : rf.cap;
   {
     ProfScope ps(g, F_PARTITION);
-    ps.bytes = 8.0 * cap_s + 16.0 * (f_small ? rf.ne : rb.ne);
-    k_partition_small<<<grid_for(g, cap_s, tb), tb, 0, g->stream>>>(Ts, cap_s, Tl, cap_l - 1,
-                                                                    (unsigned long long*)labels);
-  }
-  {
-    ProfScope ps(g, F_PARTITION);
-    ps.bytes = 8.0 * cap_l + 8.0 * (f_small ? rb.ne : rf.ne);
-    k_partition_large<<<grid_for(g, cap_l, tb), tb, 0, g->stream>>>(Tl, cap_l,
-                                                                    (unsigned long long*)labels);
+    ps.bytes = 8.0 * cap_s + 16.0 * (f_small ? rf.ne : rb.ne) + 8.0 * cap_l +
+               8.0 * (f_small ? rb.ne : rf.ne);
+    k_partition<<<grid_for(g, cap_s + cap_l, tb), tb, 0, g->stream>>>(
+        Ts, cap_s, Tl, cap_l, (unsigned long long*)labels);
   }
   PSC_CUDA(cudaGetLastError());
   return PSC_OK;

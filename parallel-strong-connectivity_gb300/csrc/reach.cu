@@ -665,7 +665,8 @@ __device__ __forceinline__ void flush_pull_counters(Counters* ctr, unsigned long
 // A warp's W words read from global memory: visited words and in-list ranges.
 // dead (optional): bitmap of vertices without in-edges in this direction,
 // which no pull can reach; they are skipped like visited ones (no in-list
-// range read) but keep their visited bit clear.
+// range read) but keep their visited bit clear, and still count as
+// unvisited (the work of the reference's dense round).
 template <int W>
 __device__ __forceinline__ void pull_load_global(uint64_t w, uint64_t nwords, uint64_t n,
                                                  const uint64_t* __restrict__ B_off,
@@ -689,7 +690,7 @@ __device__ __forceinline__ void pull_load_global(uint64_t w, uint64_t nwords, ui
       b[k] = B_off[v];
       e[k] = B_off[v + 1];
     }
-    unvisited += t[k] ? 1 : 0;
+    unvisited += v < n && !((vw[k] >> lane) & 1u) ? 1 : 0;  // dead ones included
   }
 }
 
@@ -1093,7 +1094,6 @@ struct Side {
   // unvisited vertices that some pull could still reach, after the last
   // pull round (an upper bound; UINT64_MAX before the first)
   uint64_t live = UINT64_MAX;
-  bool staged = false;  // the last pull round ran the staged kernel (counts dead vertices)
 };
 
 // Chained VGC rounds (see reach_sides): rounds per chain, and the counter set
@@ -1348,7 +1348,6 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       // in-edge): the global-memory kernel with the dead bitmap reads only
       // their ranges, where the staged one copies every range.
       const bool sparse = s.live != UINT64_MAX && 8 * s.live < n;
-      s.staged = false;
       switch (g->block) {
         case 128:
           k_reach_pull<128, kPullW><<<pull_grid<128>(g->num_sms, nwords), 128, 0, g->stream>>>(
@@ -1363,7 +1362,6 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           // they are 16-byte aligned (bulk copies)
           if (kPullStaged && !sparse && n >= kPullStagedTile + 1 && ((uintptr_t)B_off & 15) == 0 &&
               ((uintptr_t)s.vis & 15) == 0) {
-            s.staged = true;
             k_reach_pull_staged<kReachBlock, kPullW>
                 <<<pull_grid<kReachBlock, true>(g->num_sms, nwords), kReachBlock, 0, g->stream>>>(
                     B_off, B_E, fa, s.vis, fbo, n, g->ctr + s.cset);
@@ -1429,8 +1427,8 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
                                   : 16.0 * c.expanded + 5.0 * c.edges + 5.0 * c.next;
       }
       if (mode[k] == M_PULL) {
-        // unvisited minus found, minus the dead ones when the kernel counted them
-        const uint64_t dead_n = s.staged ? g->dead_count[s.backward ? 1 : 0] : 0;
+        // unvisited minus the dead ones (all unvisited but sources) minus found
+        const uint64_t dead_n = g->dead_count[s.backward ? 1 : 0];
         const uint64_t u = c.unvisited > dead_n ? c.unvisited - dead_n : 0;
         s.live = u > c.next ? u - c.next : 0;
       }

@@ -164,18 +164,14 @@ __global__ void k_bases_by_graph(const uint32_t* __restrict__ a, uint64_t na,
   }
 }
 
-// Per-graph pivot orders: P[base + i] = nz[base + feistel_k(i)] on graph k's
-// segment [npbase[k], npbase[k+1]) of nz, written as a scatter (see
-// k_perm_scatter).
-__global__ void k_perm_scatter_b(const uint32_t* __restrict__ nz, uint64_t np,
-                                 const uint32_t* __restrict__ gid, const uint64_t* __restrict__ npbase,
-                                 const FeistelKey* __restrict__ keys, uint32_t* P) {
+__global__ void k_perm_gather_b(const uint32_t* __restrict__ nz, uint64_t np,
+                                const uint32_t* __restrict__ gid, const uint64_t* __restrict__ npbase,
+                                const FeistelKey* __restrict__ keys, uint32_t* P) {
   for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < np;
        j += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t v = nz[j];
-    const uint32_t k = gid[v];
+    const uint32_t k = gid[nz[j]];
     const uint64_t base = npbase[k];
-    P[base + feistel_inv(keys[k], j - base)] = v;
+    P[j] = nz[base + feistel(keys[k], j - base)];
   }
 }
 
@@ -391,7 +387,7 @@ static int scc_batch_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t
   if (np > 0) {
     ProfScope ps(g, F_TRIM);
     ps.bytes = 12.0 * np;
-    k_perm_scatter_b<<<grid_for(g, np, tb), tb, 0, g->stream>>>(nz, np, gid, A.npbase, A.keys, P);
+    k_perm_gather_b<<<grid_for(g, np, tb), tb, 0, g->stream>>>(nz, np, gid, A.npbase, A.keys, P);
   }
   PSC_CUDA(cudaEventRecord(g->ph[1], g->stream));
   if (np > 0) {

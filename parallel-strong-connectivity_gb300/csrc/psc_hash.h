@@ -9,8 +9,7 @@
 //   hash64  — SplitMix64 finaliser (S. Vigna)
 //   rng     — SplitMix64 output for state hash64(seed) + (i+1)*golden
 //   perm    — 4-round balanced Feistel network on the smallest even-bit
-//             power-of-two domain >= k, with cycle walking into [0, k);
-//             its inverse runs the rounds backwards with the same walk
+//             power-of-two domain >= k, with cycle walking into [0, k)
 #pragma once
 #include <stdint.h>
 
@@ -79,25 +78,6 @@ PSC_HD uint64_t feistel(const FeistelKey& f, uint64_t i) {
       uint64_t nL = R;
       R = L ^ F;
       L = nL;
-    }
-    x = (L << f.half) | R;
-  } while (x >= f.k);
-  return x;
-}
-
-// Inverse of feistel: feistel_inv(f, feistel(f, i)) == i for i in [0, k).
-// The rounds run backwards, and the walk repeats the inverse while the value
-// lies outside [0, k), which retraces the forward walk.
-PSC_HD uint64_t feistel_inv(const FeistelKey& f, uint64_t j) {
-  if (f.k <= 1) return 0;
-  uint64_t x = j;
-  do {
-    uint64_t L = x >> f.half, R = x & f.hmask;
-    for (int r = 3; r >= 0; r--) {
-      uint64_t pR = L;
-      uint64_t pL = R ^ ((uint64_t)hash32((uint32_t)pR ^ f.key[r]) & f.hmask);
-      L = pL;
-      R = pR;
     }
     x = (L << f.half) | R;
   } while (x >= f.k);

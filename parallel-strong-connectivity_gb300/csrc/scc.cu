@@ -42,15 +42,11 @@ struct TrimEmit {
   }
 };
 
-// Pivot order P[i] = nz[feistel(i)] (the reference's random_shuffle of
-// NON_ZEROS, scc.hpp:303), written as a scatter: nz is read in order and
-// each entry goes to P[feistel_inv(j)], so no thread waits on a random load
-// and the scattered 4-byte writes merge in L2.
-__global__ void k_perm_scatter(const uint32_t* __restrict__ nz, uint64_t np, FeistelKey key,
-                               uint32_t* P) {
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < np;
-       j += (uint64_t)gridDim.x * blockDim.x)
-    P[feistel_inv(key, j)] = nz[j];
+__global__ void k_perm_gather(const uint32_t* __restrict__ nz, uint64_t np, FeistelKey key,
+                              uint32_t* P) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    P[i] = nz[feistel(key, i)];
 }
 
 // First-pivot labels (scc.hpp:340-349) in vertex order: a warp reads one word
@@ -184,7 +180,7 @@ static int scc_phases(psc_graph_s* g, uint64_t* labels, const psc_params_t* p) {
     FeistelKey key = feistel_key(np, p->seed);
     ProfScope ps(g, F_TRIM);
     ps.bytes = 8.0 * np;
-    k_perm_scatter<<<grid_for(g, np, tb), tb, 0, g->stream>>>(nz, np, key, P);
+    k_perm_gather<<<grid_for(g, np, tb), tb, 0, g->stream>>>(nz, np, key, P);
   }
   uint64_t label_offset = n_zeros + 1;
   PSC_CUDA(cudaEventRecord(g->ph[1], g->stream));

@@ -53,54 +53,63 @@ __global__ void k_fill_gid(const uint64_t* __restrict__ vbase, uint32_t G, uint6
     gid[v] = last_le(vbase, G + 1, v);
 }
 
-// Every edge of both directions stays inside its graph's id range: 32
-// vertices per warp step, their edges checked by a balanced warp expansion.
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
-    k_check_batch(const uint64_t* __restrict__ off, const uint32_t* __restrict__ E,
-                  const uint64_t* __restrict__ in_off, const uint32_t* __restrict__ in_E,
-                  const uint64_t* __restrict__ vbase, const uint32_t* __restrict__ gid, uint64_t n,
-                  unsigned long long* bad) {
-  __shared__ WarpExpandSmem sm[BLOCK / 32];
-  __shared__ uint32_t s_lo[BLOCK], s_hi[BLOCK];
-  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const uint64_t gw = (uint64_t)blockIdx.x * (BLOCK / 32) + wid;
-  const uint64_t nw = (uint64_t)gridDim.x * (BLOCK / 32);
+// Per-graph edge ranges of both directions: graph k's edges are
+// E[eb[k] .. eb[k+1]) with eb[k] = off[vbase[k]] (and in_E with in_off).
+__global__ void k_graph_edge_bases(const uint64_t* __restrict__ off,
+                                   const uint64_t* __restrict__ in_off,
+                                   const uint64_t* __restrict__ vbase, uint32_t G, uint64_t* eb,
+                                   uint64_t* eb_in) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= G; k += gridDim.x * blockDim.x) {
+    eb[k] = off[vbase[k]];
+    eb_in[k] = in_off[vbase[k]];
+  }
+}
+
+// Every edge stays inside its graph's id range: one coalesced pass over E in
+// chunks of kCheckChunk edges per warp.  Lane 0 finds the graph of the
+// chunk's first edge (the last k with eb[k] <= e, so empty graphs are
+// skipped); each lane then steps k forward while its edge lies past eb[k+1]
+// (edges are grouped by graph, so this is at most a few steps) and checks
+// vbase[k] <= E[e] < vbase[k+1].
+constexpr int kCheckK = 8;
+constexpr uint64_t kCheckChunk = 32 * kCheckK;
+
+__global__ void k_check_batch_edges(const uint32_t* __restrict__ E, uint64_t m,
+                                    const uint64_t* __restrict__ eb,
+                                    const uint64_t* __restrict__ vbase, uint32_t G,
+                                    unsigned long long* bad) {
+  const unsigned lane = lane_id();
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   bool found = false;
-  for (uint64_t base = gw * 32; base < n; base += nw * 32) {
-    const uint64_t u = base + lane;
-    uint32_t lo = 0, hi = 0;
-    if (u < n) {
-      const uint32_t k = gid[u];
-      lo = (uint32_t)vbase[k];
-      hi = (uint32_t)vbase[k + 1];
-    }
-    s_lo[wid * 32 + lane] = lo;
-    s_hi[wid * 32 + lane] = hi;
-    __syncwarp();
-#pragma unroll 1
-    for (int d = 0; d < 2; d++) {
-      const uint64_t* O = d ? in_off : off;
-      const uint32_t* A = d ? in_E : E;
-      uint64_t beg = 0, rem = 0;
-      if (u < n) {
-        beg = O[u];
-        rem = O[u + 1] - beg;
+  for (uint64_t c0 = gw * kCheckChunk; c0 < m; c0 += nw * kCheckChunk) {
+    uint32_t k0 = 0;
+    if (lane == 0) {
+      uint32_t lo = 0, hi = G - 1;  // last k in [0, G) with eb[k] <= c0
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&eb[mid]) <= c0)
+          lo = mid;
+        else
+          hi = mid - 1;
       }
-      // lists in pieces of at most 2^26 edges (32-bit warp scan)
-      while (__any_sync(kFull, rem > 0)) {
-        const uint32_t piece = (uint32_t)(rem < (1ull << 26) ? rem : (1ull << 26));
-        warp_expand(sm[wid], beg, piece, [&](bool act, int src, uint64_t e) {
-          if (act) {
-            const uint32_t v = __ldg(&A[e]);
-            found |= v < s_lo[wid * 32 + src] || v >= s_hi[wid * 32 + src];
-          }
-        });
-        beg += piece;
-        rem -= piece;
+      k0 = lo;
+    }
+    uint32_t k = __shfl_sync(kFull, k0, 0);
+    uint32_t v[kCheckK];
+#pragma unroll
+    for (int j = 0; j < kCheckK; j++) {
+      const uint64_t e = c0 + (uint64_t)j * 32 + lane;
+      v[j] = e < m ? __ldg(&E[e]) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kCheckK; j++) {
+      const uint64_t e = c0 + (uint64_t)j * 32 + lane;
+      if (e < m) {
+        while (k + 1 < G && __ldg(&eb[k + 1]) <= e) k++;
+        found |= v[j] < __ldg(&vbase[k]) || v[j] >= __ldg(&vbase[k + 1]);
       }
     }
-    __syncwarp();
   }
   if (__any_sync(kFull, found) && lane == 0) atomicAdd(bad, 1ull);
 }
@@ -530,9 +539,17 @@ int batch_attach(psc_graph_s* g, const uint64_t* vbase, uint32_t num_graphs, boo
   k_fill_gid<<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(g->d_vbase, num_graphs, g->n, g->d_gid);
   PSC_CUDA(cudaGetLastError());
   if (check) {
+    uint64_t* eb;
+    PSC_TRY(ensure_t(g, B_GRAPHS, 2 * ((size_t)num_graphs + 1), &eb));
     PSC_CUDA(cudaMemsetAsync(&g->ctr->aux0, 0, 8, g->stream));
-    k_check_batch<256><<<grid_for(g, g->n, 256), 256, 0, g->stream>>>(
-        g->off, g->E, g->in_off, g->in_E, g->d_vbase, g->d_gid, g->n, &g->ctr->aux0);
+    k_graph_edge_bases<<<(num_graphs + 256) / 256, 256, 0, g->stream>>>(
+        g->off, g->in_off, g->d_vbase, num_graphs, eb, eb + num_graphs + 1);
+    const unsigned cg = grid_for(g, (g->m + kCheckChunk - 1) / kCheckChunk * 32, 256);
+    k_check_batch_edges<<<cg, 256, 0, g->stream>>>(g->E, g->m, eb, g->d_vbase, num_graphs,
+                                                  &g->ctr->aux0);
+    if (g->in_E != g->E)
+      k_check_batch_edges<<<cg, 256, 0, g->stream>>>(g->in_E, g->m, eb + num_graphs + 1,
+                                                    g->d_vbase, num_graphs, &g->ctr->aux0);
     PSC_CUDA(cudaGetLastError());
     PSC_CUDA(cudaMemcpyAsync(&g->hctr->aux0, &g->ctr->aux0, 8, cudaMemcpyDeviceToHost, g->stream));
     PSC_CUDA(cudaStreamSynchronize(g->stream));

@@ -910,25 +910,33 @@ def cc_le_extra(psc, g, rank, world, args) -> dict:
     s = g.symmetrize()
     log(f"[rank {rank}] symmetrised: m = {s.m} in {time.perf_counter() - t:.1f}s")
     out = {}
-    perm = psc.random_permutation(s.n, 4)
+    # the timed calls read the permutation from and write their output to
+    # page-locked host memory, as the SCC end-to-end pass does
+    pin = Pinned(psc.cuda())
+    perm = pin.copy(psc.random_permutation(s.n, 4))
     with psc.DeviceGraph(s) as dg:
         lab = dg.cc()
-        cc_ms = min((dg.cc(), dg.stats().total_ms)[1] for _ in range(3))
+        lab_pin = pin.empty(s.n, np.uint32)
+        cc_ms = min((dg.cc(out=lab_pin), dg.stats().total_ms)[1] for _ in range(3))
         dg.set_profiling(True)
         dg.profile_reset()
         dg.cc()
         cc_roof = roofline_of(dg.profile(), 1)
         dg.set_profiling(False)
         le = dg.lelist(perm)
-        le_ms = min((dg.lelist(perm), dg.stats().total_ms)[1] for _ in range(2))
+        le_pin = pin.empty(3 * len(le), np.uint32)
+        le_ms = min((dg.lelist(perm, out=le_pin), dg.stats().total_ms)[1] for _ in range(2))
         dg.set_profiling(True)
         dg.profile_reset()
         dg.lelist(perm)
         le_roof = roofline_of(dg.profile(), 1)
         dg.set_profiling(False)
     out["connectivity"] = {"ms": cc_ms, "edges_per_s": s.m / (cc_ms / 1e3), "m_sym": s.m,
-                           "components": int(len(np.unique(lab))), "roofline": cc_roof}
-    out["lelist"] = {"ms": le_ms, "triples": int(len(le)), "perm_seed": 4, "roofline": le_roof}
+                           "components": int(len(np.unique(lab))), "roofline": cc_roof,
+                           "scope": "graph resident; labels copied to page-locked host memory"}
+    out["lelist"] = {"ms": le_ms, "triples": int(len(le)), "perm_seed": 4, "roofline": le_roof,
+                     "scope": "graph resident; permutation from and triples to page-locked "
+                              "host memory"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
         import pyoracle
@@ -955,6 +963,7 @@ def cc_le_extra(psc, g, rank, world, args) -> dict:
                 raise SystemExit("GPU LE-lists differ from the oracle's")
         if not out["connectivity"]["partition_equal_oracle"]:
             raise SystemExit("GPU connectivity partition differs from the oracle's")
+    pin.free()
     return out
 
 

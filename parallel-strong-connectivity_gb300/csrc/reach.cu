@@ -990,8 +990,12 @@ static int vgc_occupancy(psc_graph_s* g) {
   return PSC_OK;
 }
 
-// spec: speculative range loads (vgc_claim), for rounds whose frontier fits
-// the resident grid one vertex per warp
+// spec: speculative range loads (vgc_claim), for rounds whose frontier gives
+// each resident warp at most kVgcSpecChunk vertices (latency-bound rounds)
+#ifndef PSC_VGC_SPEC_CHUNK
+#define PSC_VGC_SPEC_CHUNK 8
+#endif
+constexpr uint64_t kVgcSpecChunk = PSC_VGC_SPEC_CHUNK;
 static void launch_vgc(psc_graph_s* g, unsigned blocks, const ReachSide& a, const ReachSide& b,
                        uint32_t tau, uint32_t chunk, bool spec) {
   cudaStream_t st = g->stream;
@@ -1201,11 +1205,12 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
           heavy_possible |= g->max_deg[sides[act[a]].backward ? 1 : 0] > kHeavyDeg;
         PSC_TRY(vgc_occupancy(g));
         const unsigned blocks = (unsigned)((uint64_t)g->num_sms * g->vgc_blocks);
-        // speculative range loads while the frontier fits the grid one
-        // vertex per warp (steady frontiers stay near their start size)
+        // speculative range loads while the frontier gives each warp at
+        // most kVgcSpecChunk vertices (steady frontiers stay near their
+        // start size)
         uint64_t chain_nf = 0;
         for (int a = 0; a < na; a++) chain_nf += sides[act[a]].nf;
-        const bool spec = chain_nf <= (uint64_t)blocks * (kVgcBlock / 32);
+        const bool spec = chain_nf <= (uint64_t)blocks * (kVgcBlock / 32) * kVgcSpecChunk;
         PSC_TRY(zero_counters(g));
         for (int j = 0; j < kVgcChain; j++) {
           ReachSide vg[2] = {};
@@ -1317,7 +1322,7 @@ static int reach_sides(psc_graph_s* g, Side* sides, int ns, const uint32_t* srcs
       const uint64_t chunks = (v_items + chunk - 1) / chunk;
       const uint64_t blocks = std::min(max_blocks, (chunks + kVgcBlock / 32 - 1) / (kVgcBlock / 32));
       launch_vgc(g, (unsigned)std::max<uint64_t>(1, blocks), vg[0], vg[1], tau, (uint32_t)chunk,
-                 chunk == 1);
+                 chunk <= kVgcSpecChunk);
     }
     if (np) {
       ProfScope ps(g, F_REACH_PUSH);

@@ -355,10 +355,11 @@ class DeviceGraph:
         self.last_rounds = r.value
         return dst
 
-    def cc(self, beta: float = 0.2, forest: bool = False):
+    def cc(self, beta: float = 0.2, forest: bool = False, out: np.ndarray | None = None):
         """Connected components of a symmetric graph: u32 root per vertex, and
-        with forest=True also a spanning forest as a (k, 2) u32 edge array."""
-        labels = np.empty(self.n, np.uint32)
+        with forest=True also a spanning forest as a (k, 2) u32 edge array.
+        out: optional u32[n] array (e.g. page-locked) that receives the labels."""
+        labels = out if out is not None else np.empty(self.n, np.uint32)
         if forest:
             fo = np.empty(2 * max(self.n, 1), np.uint32)
             k = C.c_uint64()
@@ -396,10 +397,18 @@ class DeviceGraph:
         self.last_rounds = r.value
         return d
 
-    def lelist(self, perm: np.ndarray, beta: float = 1.5) -> np.ndarray:
+    def lelist(self, perm: np.ndarray, beta: float = 1.5,
+               out: np.ndarray | None = None) -> np.ndarray:
         """LE-lists for priority order perm: (k, 3) u32 triples (target,
-        source vertex, distance) sorted by (target, priority)."""
+        source vertex, distance) sorted by (target, priority).  out: optional
+        u32 array of 3 * capacity entries (e.g. page-locked) that receives the
+        triples; a list longer than its capacity raises PscError."""
         perm = np.ascontiguousarray(perm, dtype=np.uint32)
+        if out is not None:
+            ln = C.c_uint64()
+            check(self._lib.psc_lelist(self.h, _ptr(perm), beta, _ptr(out), len(out) // 3,
+                                       C.byref(ln)), "psc_lelist")
+            return out[: 3 * ln.value].reshape(-1, 3)
         cap = max(16, 8 * self.n)
         while True:
             out = np.empty(3 * cap, np.uint32)

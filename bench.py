@@ -754,11 +754,18 @@ def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
 
 
 # DRAM bytes (read + write) per launch of a workload's dominant kernel family:
-# dram__bytes_read.sum + dram__bytes_write.sum averaged over the family's
-# launches in one ncu capture (a single pass) of
-# `python bench.py --ncu-step --workload W` on the current kernels.  A
-# workload without a capture of its current dominant kernel reports null.
-NCU_TRAFFIC: dict = {}
+# dram__bytes_read.sum + dram__bytes_write.sum of the family's kernels in one
+# ncu capture (a single pass) of `python bench.py --ncu-step --workload W`,
+# divided by the family's profiled scopes (the launches counted in the
+# roofline entry).  A workload without a capture of its current dominant
+# kernels reports null.
+#   scc_rmat26 / reach_pull: k_reach_pull_staged, k_reach_pull,
+#     k_pull_out_edges and k_queue_to_bitmap, 6,605 MB over 2 solves x 6 scopes
+#   scc_knn / reach_vgc: k_reach_vgc, 10,819 MB over 185 launches
+NCU_TRAFFIC: dict = {
+    ("scc_rmat26", "reach_pull"): 550.4e6,
+    ("scc_knn", "reach_vgc"): 58.5e6,
+}
 
 
 def roofline_of(prof: dict, steps: int, workload: str = "") -> dict:

@@ -41,12 +41,6 @@ constexpr int kMsVgcQueue = 512;
 constexpr int kMsK = 8;        // VGC: edges in flight per lane
 constexpr int kMsExpandK = 4;  // expand: fewer registers, more warps
 constexpr uint32_t kProbeLimit = 256;
-// Sub-rounds launched back to back, with one counter read-back, while every
-// active side of a batch runs VGC sub-rounds (most batches need two); the
-// chained sub-rounds after the first use counter sets ms_chain_set(j, side).
-constexpr int kMsChain = 2;
-constexpr int ms_chain_set(int j, int k) { return 4 + 2 * j + k; }
-static_assert(ms_chain_set(kMsChain - 1, 1) < kCounterSets, "chain counter sets");
 
 struct MsSide {
   const uint64_t* off;
@@ -61,25 +55,9 @@ struct MsSide {
   Counters* ctr;
   uint32_t vgc_budget;  // new pairs one VGC local search may insert
   // when set, the frontier size is read here instead of nin (the first
-  // sub-round of a batch started without waiting for its pivot count, or a
-  // chained sub-round reading its predecessor's count)
+  // sub-round of a batch started without waiting for its pivot count)
   const unsigned long long* nin_dev;
-  // chained sub-rounds: when set, every sub-round of the chain adds its
-  // inserts here, and the VGC budget is computed on the device from the
-  // table's load before the chain (ne_base) plus these inserts, against half
-  // the capacity (half_cap), as the host does between sub-rounds
-  unsigned long long* ne_run;
-  uint64_t ne_base, half_cap;
 };
-
-// VGC budget of a chained sub-round (see MsSide::ne_run): its share of the
-// room left below half load.
-__device__ __forceinline__ uint32_t ms_chain_budget(const MsSide& S) {
-  const uint64_t ne = S.ne_base + *(volatile const unsigned long long*)S.ne_run;
-  const uint64_t room = S.half_cap > ne ? S.half_cap - ne : 0;
-  const uint64_t share = room / (S.nin ? S.nin : 1);
-  return (uint32_t)(share < 0xFFFFFFFFull ? share : 0xFFFFFFFFull);
-}
 
 constexpr int kMsHeavyK = 4;  // heavy pairs: edges in flight per lane
 constexpr uint64_t kMsHeavyChunk = 32 * kMsHeavyK;
@@ -259,21 +237,17 @@ __device__ __forceinline__ void ms_expand_claim(WarpExpandSmem& sm, MsSrc& src, 
   __syncwarp();
 }
 
-__device__ __forceinline__ void flush_ms_counters(const MsSide& S0, const MsSide& S1,
+__device__ __forceinline__ void flush_ms_counters(Counters* c0, Counters* c1,
                                                   unsigned long long s0, unsigned long long s1,
                                                   unsigned long long r0, unsigned long long r1,
                                                   unsigned long long p0, unsigned long long p1,
                                                   unsigned long long x0, unsigned long long x1,
                                                   unsigned long long i0, unsigned long long i1) {
-  Counters* c0 = S0.ctr;
-  Counters* c1 = S1.ctr;
   i0 = warp_sum(i0);
   i1 = warp_sum(i1);
   if (lane_id() == 0) {
     if (i0) atomicAdd(&c0->inserted, i0);
     if (i1) atomicAdd(&c1->inserted, i1);
-    if (i0 && S0.ne_run) atomicAdd(S0.ne_run, i0);
-    if (i1 && S1.ne_run) atomicAdd(S1.ne_run, i1);
   }
   s0 = warp_sum(s0);
   s1 = warp_sum(s1);
@@ -361,7 +335,7 @@ __global__ void __launch_bounds__(BLOCK, (768 / BLOCK) > 0 ? (768 / BLOCK) : 1)
     }
     __syncwarp();
   }
-  flush_ms_counters(s0, s1, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1, in0, in1);
+  flush_ms_counters(s0.ctr, s1.ctr, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1, in0, in1);
 }
 
 struct MsQEnt {
@@ -469,8 +443,6 @@ __global__ void __launch_bounds__(BLOCK)
     k_ms_vgc(MsSide s0, MsSide s1, const uint64_t* __restrict__ labels, uint32_t tau) {
   if (s0.nin_dev) s0.nin = *s0.nin_dev;
   if (s1.nin_dev) s1.nin = *s1.nin_dev;
-  if (s0.ne_run) s0.vgc_budget = ms_chain_budget(s0);
-  if (s1.ne_run) s1.vgc_budget = ms_chain_budget(s1);
   __shared__ WarpExpandSmem sm[BLOCK / 32];
   __shared__ MsQEnt sq[BLOCK / 32][QCAP];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -624,7 +596,7 @@ __global__ void __launch_bounds__(BLOCK)
     }
     __syncwarp();
   }
-  flush_ms_counters(s0, s1, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1, in0, in1);
+  flush_ms_counters(s0.ctr, s1.ctr, sc0, sc1, rq0, rq1, pr0, pr1, ex0, ex1, in0, in1);
 }
 
 // Heavy pairs of both sides: the chunks of a side's heavy list are cut into
@@ -715,7 +687,6 @@ __global__ void __launch_bounds__(BLOCK)
     const unsigned long long pr = warp_sum((unsigned long long)probes);
     if (lane == 0) {
       if (ins) atomicAdd(&S.ctr->inserted, ins);
-      if (ins && S.ne_run) atomicAdd(S.ne_run, ins);
       if (scanned) atomicAdd(&S.ctr->heavy_edges, scanned);
       if (pr) atomicAdd(&S.ctr->heavy_probes, pr);
       if (requeued) {
@@ -775,9 +746,6 @@ MsSide ms_args(psc_graph_s* g, const MsState& s) {
   r.hflag = (uint32_t*)g->bufs[s.f_slot].p;
   r.ctr = g->ctr + s.cset;
   r.nin_dev = nullptr;
-  r.ne_run = nullptr;
-  r.ne_base = 0;
-  r.half_cap = 0;
   // VGC local searches share the room left below half load, so one
   // sub-round cannot fill the table
   const uint64_t room = s.cap / 2 > s.ne ? s.cap / 2 - s.ne : 0;
@@ -826,7 +794,7 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
   // and the heavy walk follows it whenever some vertex could be heavy
   bool first_async = async && async->nf_dev;
   bool heavy_possible = false;
-  if (first_async || (local && kMsChain > 1)) {
+  if (first_async) {
     PSC_TRY(ensure_max_degrees(g));
     heavy_possible = g->max_deg[0] > kHeavyDeg || g->max_deg[1] > kHeavyDeg;
   }
@@ -878,15 +846,6 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       }
       hv[nh++] = a;
     }
-    // every active side in VGC mode: a chain of kMsChain sub-rounds
-    const bool chain = kMsChain > 1 && nv > 0 && ne == 0;
-    if (chain)
-      for (int a = 0; a < nv; a++) {
-        const MsState& s = st[vg[a].ctr == g->ctr + st[0].cset ? 0 : 1];
-        vg[a].ne_run = &g->ctr[3].pad[a];  // staging set 3, zeroed above
-        vg[a].ne_base = s.ne;
-        vg[a].half_cap = s.cap / 2;
-      }
     if (nv) {
       ProfScope ps(g, F_MS_VGC);
       // a resident grid, one pair per warp at a time
@@ -900,38 +859,6 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
           std::min(max_blocks, (v_items + kMsVgcBlock / 32 - 1) / (kMsVgcBlock / 32));
       k_ms_vgc<kMsVgcBlock, kMsVgcQueue><<<(unsigned)std::max<uint64_t>(1, blocks), kMsVgcBlock, 0,
                                            g->stream>>>(vg[0], vg[1], labels, tau);
-    }
-    if (chain) {
-      // the chained sub-rounds read their frontier from the previous one's
-      // output buffer and count; heavy pairs are walked after each one
-      // (the heavy kernel returns at once when none were listed)
-      MsSide prev[2] = {vg[0], vg[1]};
-      for (int j = 1; j < kMsChain; j++) {
-        if (heavy_possible) {
-          ProfScope ps(g, F_HEAVY);
-          k_ms_heavy<kMsBlock><<<g->num_sms * 4, kMsBlock, 0, g->stream>>>(prev[0], prev[1], labels);
-        }
-        MsSide cur[2] = {};
-        for (int a = 0; a < nv; a++) {
-          cur[a] = prev[a];
-          cur[a].Fin = prev[a].Fout;
-          cur[a].Fout = const_cast<uint64_t*>(prev[a].Fin);
-          cur[a].nin = 0;
-          cur[a].nin_dev = &prev[a].ctr->next;
-          cur[a].ctr = g->ctr + ms_chain_set(j, vg[a].ctr == g->ctr + st[0].cset ? 0 : 1);
-        }
-        ProfScope ps(g, F_MS_VGC);
-        // the whole resident grid: the frontier size is known on the device only
-        k_ms_vgc<kMsVgcBlock, kMsVgcQueue>
-            <<<(unsigned)((uint64_t)g->num_sms * g->ms_vgc_blocks), kMsVgcBlock, 0, g->stream>>>(
-                cur[0], cur[1], labels, tau);
-        prev[0] = cur[0];
-        prev[1] = cur[1];
-      }
-      if (heavy_possible) {
-        ProfScope ps(g, F_HEAVY);
-        k_ms_heavy<kMsBlock><<<g->num_sms * 4, kMsBlock, 0, g->stream>>>(prev[0], prev[1], labels);
-      }
     }
     if (ne) {
       ProfScope ps(g, F_MS_EXPAND);
@@ -948,7 +875,7 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       }
     }
     PSC_CUDA(cudaGetLastError());
-    if (first_async && heavy_possible && !chain) {  // returns at once when no pair was listed
+    if (first_async && heavy_possible) {  // returns at once when no pair was listed
       ProfScope ps(g, F_HEAVY);
       k_ms_heavy<kMsBlock><<<g->num_sms * 4, kMsBlock, 0, g->stream>>>(hv[0], hv[1], labels);
     }
@@ -970,7 +897,7 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
     }
     // Heavy pairs are rare: the grid-wide walk is launched only for a round
     // that queued some, then the counters are read again.
-    if (!first_async && !chain &&
+    if (!first_async &&
         ((st[0].nf && g->hctr[st[0].cset].heavy) || (st[1].nf && g->hctr[st[1].cset].heavy))) {
       {
         ProfScope ps(g, F_HEAVY);
@@ -1016,32 +943,6 @@ int ms_pair(psc_graph_s* g, const uint32_t* front, uint64_t n_front, uint64_t la
       s.grow = c.fail > 0;
       std::swap(g->bufs[s.a_slot], g->bufs[s.b_slot]);
       s.nf = c.next;
-      auto heavy_bytes = [&](const Counters& x) {
-        if (g->profiling && chain && heavy_possible)
-          g->prof[F_HEAVY].bytes +=
-              28.0 * (x.heavy >> kPackShift) + 12.0 * x.heavy_edges + 8.0 * x.heavy_probes;
-      };
-      if (!first_async) heavy_bytes(c);  // (the first sub-round of an async batch is counted above)
-      // the chained sub-rounds of this side, in order
-      for (int j = 1; chain && j < kMsChain; j++) {
-        const Counters& cj = g->hctr[ms_chain_set(j, k)];
-        heavy_bytes(cj);
-        if (s.nf) {
-          g->stats.subrounds++;
-          if (g->profiling)
-            g->prof[F_MS_VGC].bytes +=
-                8.0 * s.nf + 16.0 * cj.expanded + 12.0 * cj.edges + 8.0 * cj.probes + 8.0 * cj.next;
-          if (trace_on())
-            std::fprintf(stderr, "ms side %d mode vgc-chain nf %llu next %llu edges %llu probes %llu "
-                         "expanded %llu cap %llu ne %llu\n",
-                         k, (unsigned long long)s.nf, cj.next, cj.edges, cj.probes, cj.expanded,
-                         (unsigned long long)s.cap, (unsigned long long)s.ne);
-        }
-        s.ne += cj.inserted;
-        s.grow = s.grow || cj.fail > 0;
-        std::swap(g->bufs[s.a_slot], g->bufs[s.b_slot]);
-        s.nf = cj.next;
-      }
     }
     first_async = false;
   }

@@ -59,6 +59,16 @@ def test_cc_generated(kind, size, seed):
     check_forest(s.n, ref, forest)
 
 
+def test_cc_caller_buffer():
+    """Labels written into a caller array equal the allocating call's."""
+    s = generated("rmat", 12, 5).symmetrize()
+    with psc.DeviceGraph(s) as dg:
+        ref = dg.cc()
+        buf = np.zeros(s.n, np.uint32)
+        assert dg.cc(out=buf) is buf
+        assert np.array_equal(buf, ref)
+
+
 def test_cc_many_components():
     # disjoint cycles of various sizes plus isolated vertices
     src, dst = [], []

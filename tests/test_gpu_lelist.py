@@ -51,6 +51,22 @@ def test_lelist_generated(kind, size, seed):
             assert np.array_equal(dg.lelist(perm, beta), ref)
 
 
+def test_lelist_caller_buffer():
+    """Triples written into a caller array (what bench.py passes, page-locked),
+    equal to the allocating call; a too-small array is refused with
+    PSC_ERR_CAPACITY."""
+    s = generated("rmat", 12, 5).symmetrize()
+    perm = psc.random_permutation(s.n, 9)
+    with psc.DeviceGraph(s) as dg:
+        ref = dg.lelist(perm)
+        buf = np.full(3 * len(ref) + 7, 0xFFFFFFFF, np.uint32)
+        got = dg.lelist(perm, out=buf)
+        assert np.array_equal(got, ref)
+        assert np.all(buf[3 * len(ref):] == 0xFFFFFFFF)
+        with pytest.raises(psc.PscError):
+            dg.lelist(perm, out=np.empty(3 * (len(ref) - 1), np.uint32))
+
+
 def hub_graph(n, sizes, seed):
     """Symmetric graph: hubs 0..len(sizes) with the given numbers of random
     neighbours over a sparse random backbone."""

@@ -761,10 +761,10 @@ def cpu_baseline_batch(g, vb, seeds, sample, budget_s: float = 15.0) -> dict:
 # kernels reports null.
 #   scc_rmat26 / reach_pull: k_reach_pull_staged, k_reach_pull,
 #     k_pull_out_edges and k_queue_to_bitmap, 6,605 MB over 2 solves x 6 scopes
-#   scc_knn / reach_vgc: k_reach_vgc, 10,819 MB over 185 launches
+#   scc_knn / reach_vgc: k_reach_vgc, 10,912 MB over 185 launches
 NCU_TRAFFIC: dict = {
     ("scc_rmat26", "reach_pull"): 550.4e6,
-    ("scc_knn", "reach_vgc"): 58.5e6,
+    ("scc_knn", "reach_vgc"): 59.0e6,
 }
 
 

@@ -206,6 +206,9 @@ int cuda_status(cudaError_t e);
 // Round tracing to stderr when the environment sets PSC_TRACE (the reference
 // prints per-round frontier sizes under DEBUG, src/reach.hpp:218-239).
 bool trace_on();
+// Per-batch server timeline only (PSC_TRACE_SERVER, or PSC_TRACE), without the
+// per-round lines and their waits.
+bool trace_server_on();
 void set_last_cuda_error(cudaError_t e);
 
 // Returns a device pointer of at least `bytes` for slot `b` (contents of a

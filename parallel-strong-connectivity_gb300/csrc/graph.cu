@@ -72,6 +72,14 @@ bool trace_on() {
   return on;
 }
 
+bool trace_server_on() {
+  static const bool on = [] {
+    const char* v = std::getenv("PSC_TRACE_SERVER");
+    return trace_on() || (v && *v && *v != '0');
+  }();
+  return on;
+}
+
 int cuda_status(cudaError_t e) {
   g_last_cuda = e;
   if (e == cudaErrorMemoryAllocation) return PSC_ERR_OOM;

@@ -144,6 +144,7 @@ struct psc_server_s {
   uint64_t upload_turn = 0;
   bool stop = false;
   psc_server_stats_t stats{};
+  std::chrono::steady_clock::time_point t_epoch = std::chrono::steady_clock::now();  // trace times
 };
 
 namespace psc {
@@ -201,7 +202,7 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t tick
   }
   const uint64_t n = vbase[R], m = ebase[R];
   if (n >= 0xFFFFFFFFull) return PSC_ERR_TOO_LARGE;
-  const bool tr = trace_on();
+  const bool tr = trace_server_on();
   std::vector<std::pair<const char*, double>> marks;
   const auto t_begin = Clock::now();
   psc_graph_s* g = nullptr;
@@ -221,6 +222,8 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t tick
     bool with_t = kind == PSC_REQ_SCC;
     for (uint32_t k = 0; k < R; k++) with_t = with_t && B[k]->in_off != nullptr;
     turn.wait();
+    if (tr)  // host time the upload turn came (no stream wait)
+      marks.emplace_back("turn", std::chrono::duration<double, std::milli>(Clock::now() - t_begin).count());
     for (uint32_t k = 0; k < R; k++) {
       PSC_CUDA(cudaMemcpyAsync(g->off + vbase[k], B[k]->off, B[k]->n * 8, cudaMemcpyDefault, g->stream));
       if (B[k]->m)
@@ -253,6 +256,9 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t tick
       PSC_CUDA(cudaGetLastError());
       PSC_TRY(read_counters(g));  // the copies are done: the link is the next batch's
       turn.release();
+      if (tr)
+        marks.emplace_back("released",
+                           std::chrono::duration<double, std::milli>(Clock::now() - t_begin).count());
       if (g->hctr[2].aux0) {
         std::vector<uint64_t> hf(R);
         PSC_CUDA(cudaMemcpyAsync(hf.data(), flags, R * 8, cudaMemcpyDeviceToHost, g->stream));
@@ -299,8 +305,9 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t tick
   *launches = g->stats.kernel_launches;
   psc_graph_free(g);
   if (tr) {
-    std::fprintf(stderr, "server batch kind %d requests %u n %llu m %llu:", kind, R,
-                 (unsigned long long)n, (unsigned long long)m);
+    std::fprintf(stderr, "server batch at %.2f ms ticket %llu kind %d requests %u n %llu m %llu:",
+                 std::chrono::duration<double, std::milli>(t_begin - S->t_epoch).count(),
+                 (unsigned long long)ticket, kind, R, (unsigned long long)n, (unsigned long long)m);
     for (auto& mk : marks) std::fprintf(stderr, " %s %.2f", mk.first, mk.second);
     std::fprintf(stderr, " freed %.2f ms\n",
                  std::chrono::duration<double, std::milli>(Clock::now() - t_begin).count());

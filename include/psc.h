@@ -183,15 +183,17 @@ int psc_tune_scc(psc_graph_t g, const uint64_t* seeds, uint32_t reps, psc_params
  * with continuous batching under a device-memory budget.  No counterpart in
  * the reference.
  *
- * Submitted requests queue in arrival order.  Each of `workers` threads (one
- * CUDA stream each) takes, whenever it is free, the queued requests of the
+ * Submitted requests queue in arrival order.  Each of 2 * `workers` threads
+ * (one CUDA stream per batch) takes, whenever it is free, the queued requests of the
  * kind at the head of the queue while their estimated device footprint fits
  * hbm_budget minus what running batches hold (at most max_batch requests
  * and max_batch_edges edges), packs them into one batch on the device, solves
  * it with the batched path and copies each member's labels to its caller.
- * Batches copy their inputs to the device one after another in the order
- * they were taken, so each reaches the device at full link speed and solves
- * while later batches copy.  Requests arriving while
+ * At most `workers` batches solve at a time; the other threads' batches copy
+ * their inputs meanwhile and wait for a solve slot, so the host link stays
+ * busy while every slot solves.  Batches copy their inputs to the device one
+ * after another in the order they were taken, so each reaches the device at
+ * full link speed and solves while later batches copy.  Requests arriving while
  * batches run are admitted as workers and budget free up; their work overlaps
  * the running batches.  A request larger than the whole budget is refused at
  * submission (PSC_ERR_TOO_LARGE).  Results do not depend on the mix: SCC
@@ -202,7 +204,7 @@ typedef struct psc_server_s* psc_server_t;
 #define PSC_REQ_CC 1  /* symmetric CSR; labels_out u32[n] as psc_cc */
 typedef struct {
   uint64_t hbm_budget;  /* device bytes admitted batches may hold (120 GiB) */
-  uint32_t workers;     /* batches in flight, one stream each (4) */
+  uint32_t workers;     /* batches solving at a time (4); twice as many in flight */
   uint32_t max_batch;   /* requests per batch (4096) */
   double cc_beta;       /* LDD beta of connectivity requests (0.2) */
   psc_params_t scc;     /* SCC parameters; the seed comes with each request */

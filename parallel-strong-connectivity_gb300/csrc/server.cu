@@ -142,6 +142,12 @@ struct psc_server_s {
   std::condition_variable upload_cv;
   uint64_t next_ticket = 0;
   uint64_t upload_turn = 0;
+  // Solve slots: cfg.workers batches solve at a time; twice as many worker
+  // threads run, so while every slot is busy the others copy their inputs
+  // ahead (measured: with one thread per slot the link idled ~24 ms of a
+  // 193 ms saturated stream, each time all workers were solving).
+  std::condition_variable solve_cv;
+  uint32_t solving = 0;
   bool stop = false;
   psc_server_stats_t stats{};
   std::chrono::steady_clock::time_point t_epoch = std::chrono::steady_clock::now();  // trace times
@@ -182,6 +188,28 @@ struct UploadTurn {
   ~UploadTurn() { release(); }
 };
 
+// A solve slot, taken after the batch's copies and released when its labels
+// are out.  The wait is bounded like the upload turn's: a batch that waited
+// kTurnWait solves anyway.
+struct SolveSlot {
+  psc_server_s* S;
+  bool held = false;
+  void take() {
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->solve_cv.wait_for(lk, kTurnWait, [&] { return S->solving < S->cfg.workers; });
+    S->solving++;
+    held = true;
+  }
+  ~SolveSlot() {
+    if (!held) return;
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->solving--;
+    }
+    S->solve_cv.notify_one();
+  }
+};
+
 uint64_t take_ticket(psc_server_s* S) {
   std::lock_guard<std::mutex> lk(S->mu);
   return S->next_ticket++;
@@ -194,6 +222,7 @@ uint64_t take_ticket(psc_server_s* S) {
 int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t ticket,
               uint64_t* launches, std::vector<char>* bad_out) {
   UploadTurn turn{S, ticket};
+  SolveSlot slot{S};
   const uint32_t R = (uint32_t)B.size();
   std::vector<uint64_t> vbase(R + 1, 0), ebase(R + 1, 0);
   for (uint32_t k = 0; k < R; k++) {
@@ -278,6 +307,9 @@ int run_batch(psc_server_s* S, std::vector<Request*>& B, int kind, uint64_t tick
     }
     PSC_CUDA(cudaGetLastError());
     PSC_TRY(stamp("upload"));
+    slot.take();
+    if (tr)
+      marks.emplace_back("slot", std::chrono::duration<double, std::milli>(Clock::now() - t_begin).count());
     // SCC needs the in-edges: built on the device when they did not come along
     if (kind == PSC_REQ_SCC && !with_t) PSC_TRY(build_transpose(g));
     PSC_TRY(batch_attach(g, vbase.data(), R, false));
@@ -451,7 +483,7 @@ extern "C" int psc_server_create(const psc_server_config_t* cfg, psc_server_t* o
   S->cfg = c;
   S->device = dev;
   S->urgent_priority = greatest;
-  for (uint32_t w = 0; w < c.workers; w++) S->workers.emplace_back(worker_loop, S);
+  for (uint32_t w = 0; w < 2 * c.workers; w++) S->workers.emplace_back(worker_loop, S);
   *out = S;
   return PSC_OK;
 }

@@ -122,13 +122,20 @@ def test_server_malformed_request_fails_alone_in_its_batch(kind):
     E[7] = b.n + 2
     bad = psc.HostGraph(b.n, b.m, b.off, E, symmetric=b.symmetric)
     blocker = sym(psc.HostGraph.knn(1_000_000, 5, seed=9))
-    with psc.Server(workers=1, max_batch=8) as srv:
-        # the worker is busy with the blocker while the next three queue up,
-        # so they are taken as one batch
+    n, m = blocker.n, blocker.m
+    # the server's footprint estimate of one blocker (SCC: transpose built on
+    # the device, as submit sends none here)
+    x = 16 * (n + 1) + 22 * m + 168 * n if kind == SCC else 8 * (n + 1) + 4 * m + 64 * n
+    # room for one blocker and a half: the second blocker waits until the
+    # first is done, the three small requests queue behind it, and all four
+    # are taken as one batch (whichever worker thread takes them)
+    with psc.Server(workers=1, max_batch=8, hbm_budget=int(1.5 * x)) as srv:
         r0 = srv.submit(blocker, kind, 1)
+        r1 = srv.submit(blocker, kind, 2)
         ids = [srv.submit(goods[0], kind, 11), srv.submit(bad, kind, 12),
                srv.submit(goods[1], kind, 13)]
         srv.wait(r0)
+        srv.wait(r1)
         outs = []
         for rid in (ids[0], ids[2]):
             lab, info = srv.wait(rid)

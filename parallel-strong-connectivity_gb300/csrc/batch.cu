@@ -173,14 +173,46 @@ __global__ void k_bases_by_graph(const uint32_t* __restrict__ a, uint64_t na,
   }
 }
 
+// Per-graph pivot orders: P[j] = nz[base + feistel_k(j - base)] on graph k's
+// segment [npbase[k], npbase[k+1]) of nz, with the lanes of a warp refilled as
+// their walks land, as in k_perm_gather.
+constexpr uint64_t kPermChunkB = 32 * 32;
+
 __global__ void k_perm_gather_b(const uint32_t* __restrict__ nz, uint64_t np,
                                 const uint32_t* __restrict__ gid, const uint64_t* __restrict__ npbase,
                                 const FeistelKey* __restrict__ keys, uint32_t* P) {
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < np;
-       j += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t k = gid[nz[j]];
-    const uint64_t base = npbase[k];
-    P[j] = nz[base + feistel(keys[k], j - base)];
+  const unsigned lane = lane_id();
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c0 = gw * kPermChunkB; c0 < np; c0 += nw * kPermChunkB) {
+    const uint64_t c1 = c0 + kPermChunkB < np ? c0 + kPermChunkB : np;
+    uint64_t next = c0 + 32;
+    uint64_t j = c0 + lane, x = 0, base = 0;
+    FeistelKey key{};
+    bool act = j < c1;
+    auto start = [&]() {  // element j: its graph's key and segment base
+      const uint32_t k = gid[nz[j]];
+      base = npbase[k];
+      key = keys[k];
+      x = j - base;
+    };
+    if (act) start();
+    while (__any_sync(kFull, act)) {
+      bool landed = false;
+      if (act) {
+        // a segment of at most one element maps to itself (feistel's k <= 1)
+        x = key.k <= 1 ? 0 : feistel_net(key, x);
+        landed = x < key.k;
+        if (landed) P[j] = nz[base + x];
+      }
+      const uint32_t lm = __ballot_sync(kFull, landed);
+      if (landed) {
+        j = next + __popc(lm & ((1u << lane) - 1));
+        act = j < c1;
+        if (act) start();
+      }
+      next += __popc(lm);
+    }
   }
 }
 

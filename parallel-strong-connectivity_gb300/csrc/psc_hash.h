@@ -67,19 +67,24 @@ PSC_HD FeistelKey feistel_key(uint64_t k, uint64_t seed) {
   return f;
 }
 
-// Bijection on [0, k).
+// One pass of the 4-round network over the power-of-two domain.
+PSC_HD uint64_t feistel_net(const FeistelKey& f, uint64_t x) {
+  uint64_t L = x >> f.half, R = x & f.hmask;
+  for (int r = 0; r < 4; r++) {
+    uint64_t F = (uint64_t)hash32((uint32_t)R ^ f.key[r]) & f.hmask;
+    uint64_t nL = R;
+    R = L ^ F;
+    L = nL;
+  }
+  return (L << f.half) | R;
+}
+
+// Bijection on [0, k): the network repeated until the value falls in [0, k).
 PSC_HD uint64_t feistel(const FeistelKey& f, uint64_t i) {
   if (f.k <= 1) return 0;
   uint64_t x = i;
   do {
-    uint64_t L = x >> f.half, R = x & f.hmask;
-    for (int r = 0; r < 4; r++) {
-      uint64_t F = (uint64_t)hash32((uint32_t)R ^ f.key[r]) & f.hmask;
-      uint64_t nL = R;
-      R = L ^ F;
-      L = nL;
-    }
-    x = (L << f.half) | R;
+    x = feistel_net(f, x);
   } while (x >= f.k);
   return x;
 }

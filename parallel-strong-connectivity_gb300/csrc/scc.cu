@@ -42,11 +42,41 @@ struct TrimEmit {
   }
 };
 
+// Pivot order P[i] = nz[feistel(i)] (the reference's random_shuffle of
+// NON_ZEROS, scc.hpp:303).  The permutation walks its cycle until it lands
+// in [0, np): 2.5 network passes per element on average for 27 M elements on
+// a 2^26 domain, but the slowest of a warp's 32 lanes takes ~8.  So a warp
+// takes a chunk of kPermChunk elements, and a lane that lands takes the
+// chunk's next element at once (one network pass per loop step): the warp
+// waits only at the end of its chunk.
+constexpr uint64_t kPermChunk = 32 * 32;
+
 __global__ void k_perm_gather(const uint32_t* __restrict__ nz, uint64_t np, FeistelKey key,
                               uint32_t* P) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np;
-       i += (uint64_t)gridDim.x * blockDim.x)
-    P[i] = nz[feistel(key, i)];
+  const unsigned lane = lane_id();
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c0 = gw * kPermChunk; c0 < np; c0 += nw * kPermChunk) {
+    const uint64_t c1 = c0 + kPermChunk < np ? c0 + kPermChunk : np;
+    uint64_t next = c0 + 32;  // first element no lane has taken yet
+    uint64_t i = c0 + lane, x = i;
+    bool act = i < c1;
+    while (__any_sync(kFull, act)) {
+      bool landed = false;
+      if (act) {
+        x = feistel_net(key, x);
+        landed = x < np;
+        if (landed) P[i] = nz[x];
+      }
+      const uint32_t lm = __ballot_sync(kFull, landed);
+      if (landed) {
+        i = next + __popc(lm & ((1u << lane) - 1));
+        x = i;
+        act = i < c1;
+      }
+      next += __popc(lm);
+    }
+  }
 }
 
 // First-pivot labels (scc.hpp:340-349) in vertex order: a warp reads one word

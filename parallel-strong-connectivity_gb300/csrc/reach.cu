@@ -15,7 +15,11 @@
 //   pull: the frontier is a bitmap; each warp owns 32 consecutive unvisited
 //         vertices and scans their in-edges until a frontier bit is found,
 //         then writes the visited / next-frontier words with one store
-//         (the reference's dense_update, no atomics).
+//         (the reference's dense_update, no atomics).  Dense rounds stage
+//         each warp's next offsets and visited words in shared memory with
+//         bulk asynchronous copies; once few reachable vertices remain, the
+//         global-memory kernel skips vertices without in-edges (a bitmap per
+//         direction, built once per handle), which no pull can reach.
 // The push/pull switch follows the reference's rule (REACH::judge, reach.hpp:86-112):
 // push while frontier vertices + their out-edges < m / pull_div (20).  After a
 // push round the out-edge count is exact (gathered by the kernels); after a
